@@ -1,0 +1,403 @@
+"""Host-side mirror of the reference's exact-path API over the C ABI.
+
+Maximilien-Hantonne/Bose-Hubbard-Phase-Transition exposes its exact path as
+C++ functions (``BH::fixed_set_basis``, ``BH::fixed_bosons_hamiltonian``,
+``Neighbours``, ``Op::IRLM_eigen``, ``Analysis::gap_ratios``).  This module
+keeps those names, argument meanings and error behaviour and routes every
+computation through ``libbhgb300.so`` (include/bh_gb300.h): nothing here
+computes on the CPU except argument marshalling.  The library must load; if it
+is missing it is built, and if that fails the import fails loudly.
+
+Layout conventions: a basis is returned as the reference returns it
+(tags[D], basis[m, D]); sparse matrices are scipy CSR in the reference's
+column order; eigenvectors are columns.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import build as _build
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+
+BH_OK, BH_ERR_ARG, BH_ERR_NOCONV, BH_ERR_BREAKDOWN, BH_ERR_TIMEOUT, BH_ERR_CUDA, BH_ERR_NOMEM = range(7)
+ORDER_REFERENCE, ORDER_LEX = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+
+
+class BHError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(msg)
+        self.code = code
+
+
+class bh_solver_opts(C.Structure):
+    _fields_ = [
+        ("nev", C.c_int), ("ncv", C.c_int), ("block", C.c_int), ("precision", C.c_int),
+        ("max_restarts", C.c_int), ("tol", C.c_double), ("seed", C.c_uint64),
+        ("want_vectors", C.c_int), ("order", C.c_int),
+    ]
+
+
+class bh_solve_info(C.Structure):
+    _fields_ = [
+        ("nconv", C.c_int), ("restarts", C.c_int), ("matvecs", C.c_int64),
+        ("max_resid", C.c_double), ("seconds", C.c_double),
+    ]
+
+
+EXPORTS = [
+    "bh_last_error", "bh_version", "bh_neighbours_chain", "bh_neighbours_square",
+    "bh_neighbours_cube", "bh_dimension", "bh_basis_create", "bh_basis_destroy",
+    "bh_basis_info", "bh_basis_copy", "bh_basis_index", "bh_hamiltonian_create",
+    "bh_hamiltonian_destroy", "bh_hamiltonian_nnz", "bh_hamiltonian_csr",
+    "bh_hamiltonian_apply", "bh_solver_opts_default", "bh_eigsh", "bh_eigsh_csr",
+    "bh_eigsh_batch", "bh_gap_ratios", "bh_spdm", "bh_phase_map",
+]
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load() -> C.CDLL:
+    """Load (building first if needed) libbhgb300.so and declare its signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build()
+    L = C.CDLL(path)
+    vp, i32p, i64p, f64p = C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_double)
+    L.bh_last_error.restype = C.c_char_p
+    L.bh_version.restype = C.c_int
+    for f in ("bh_neighbours_chain", "bh_neighbours_square", "bh_neighbours_cube"):
+        getattr(L, f).argtypes = [C.c_int, C.c_int, vp, vp, C.c_int, C.POINTER(C.c_int)]
+    L.bh_dimension.argtypes = [C.c_int, C.c_int, i64p]
+    L.bh_basis_create.argtypes = [C.c_int, C.c_int, C.POINTER(vp)]
+    L.bh_basis_destroy.argtypes = [vp]
+    L.bh_basis_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), i64p]
+    L.bh_basis_copy.argtypes = [vp, vp, vp, vp, vp]
+    L.bh_basis_index.argtypes = [vp, C.c_int64, vp, vp]
+    L.bh_hamiltonian_create.argtypes = [vp, vp, vp, C.POINTER(vp)]
+    L.bh_hamiltonian_destroy.argtypes = [vp]
+    L.bh_hamiltonian_nnz.argtypes = [vp, i64p]
+    L.bh_hamiltonian_csr.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, vp, vp, vp]
+    L.bh_hamiltonian_apply.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, vp, vp]
+    L.bh_solver_opts_default.argtypes = [C.POINTER(bh_solver_opts)]
+    L.bh_solver_opts_default.restype = None
+    L.bh_eigsh.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.POINTER(bh_solver_opts),
+                           vp, vp, vp, C.POINTER(bh_solve_info)]
+    L.bh_eigsh_csr.argtypes = [C.c_int64, vp, vp, vp, C.POINTER(bh_solver_opts), vp, vp, vp,
+                               C.POINTER(bh_solve_info)]
+    L.bh_eigsh_batch.argtypes = [vp, C.c_int, vp, vp, vp, C.POINTER(bh_solver_opts), vp, vp, vp,
+                                 C.POINTER(bh_solve_info)]
+    L.bh_gap_ratios.argtypes = [C.c_int, vp, vp, f64p]
+    L.bh_spdm.argtypes = [vp, C.c_int, vp, vp]
+    L.bh_phase_map.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, vp, C.c_int, vp, vp, vp]
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _check(rc: int):
+    if rc != BH_OK:
+        msg = load().bh_last_error().decode()
+        if rc == BH_ERR_NOCONV:
+            raise BHError(rc, msg or "Eigenvalue computation failed.")
+        if rc == BH_ERR_ARG:
+            err = BHError(rc, msg)
+            raise ValueError(msg) from err
+        raise BHError(rc, msg)
+
+
+def default_opts(**kw) -> bh_solver_opts:
+    o = bh_solver_opts()
+    load().bh_solver_opts_default(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+# ---------------------------------------------------------------------------
+# Neighbours (neighbours.hpp:20-58)
+# ---------------------------------------------------------------------------
+class Neighbours:
+    """Neighbour lists of a chain / square / cube lattice of m sites."""
+
+    def __init__(self, m: int):
+        self.m = int(m)
+        self._lists: list[list[int]] = [[] for _ in range(self.m)]
+
+    def _fill(self, fn, closed: bool):
+        L = load()
+        off = np.zeros(self.m + 1, np.int32)
+        cnt = C.c_int(0)
+        _check(getattr(L, fn)(self.m, int(bool(closed)), _ptr(off), None, 0, C.byref(cnt)))
+        nb = np.zeros(max(cnt.value, 1), np.int32)
+        _check(getattr(L, fn)(self.m, int(bool(closed)), _ptr(off), _ptr(nb), len(nb), C.byref(cnt)))
+        self._lists = [nb[off[i]:off[i + 1]].tolist() for i in range(self.m)]
+
+    def chain_neighbours(self, closed: bool = True):
+        self._fill("bh_neighbours_chain", closed)
+
+    def square_neighbours(self, closed: bool = True):
+        self._fill("bh_neighbours_square", closed)
+
+    def cube_neighbours(self, closed: bool = True):
+        self._fill("bh_neighbours_cube", closed)
+
+    def getNeighbours(self) -> list[list[int]]:
+        return [list(x) for x in self._lists]
+
+
+def flatten_neighbours(lists) -> tuple[np.ndarray, np.ndarray]:
+    off = np.zeros(len(lists) + 1, np.int32)
+    for i, l in enumerate(lists):
+        off[i + 1] = off[i] + len(l)
+    flat = np.array([j for l in lists for j in l], np.int32) if off[-1] else np.zeros(1, np.int32)
+    return off, flat
+
+
+# ---------------------------------------------------------------------------
+# device-resident basis + Hamiltonian (the engine objects)
+# ---------------------------------------------------------------------------
+class Basis:
+    """Fixed-n Fock basis built on the device (BH::fixed_set_basis)."""
+
+    def __init__(self, m: int, n: int):
+        L = load()
+        self._h = C.c_void_p()
+        _check(L.bh_basis_create(int(m), int(n), C.byref(self._h)))
+        mm, nn, D = C.c_int(), C.c_int(), C.c_int64()
+        _check(L.bh_basis_info(self._h, C.byref(mm), C.byref(nn), C.byref(D)))
+        self.m, self.n, self.D = mm.value, nn.value, D.value
+        self._col_of_lex = None
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.bh_basis_destroy(self._h)
+            self._h = None
+
+    def copy(self, tags=True, basis=True):
+        t = np.zeros(self.D) if tags else None
+        b = np.zeros(self.D * self.m) if basis else None
+        _check(load().bh_basis_copy(self._h, _ptr(t), _ptr(b), None, None))
+        return t, (None if b is None else b.reshape(self.D, self.m).T.copy())
+
+    def orders(self):
+        a = np.zeros(self.D, np.int32)
+        b = np.zeros(self.D, np.int32)
+        _check(load().bh_basis_copy(self._h, None, None, _ptr(a), _ptr(b)))
+        return a, b
+
+    def index(self, occ: np.ndarray) -> np.ndarray:
+        occ = np.ascontiguousarray(np.atleast_2d(occ), np.uint8)
+        out = np.zeros(occ.shape[0], np.int32)
+        _check(load().bh_basis_index(self._h, occ.shape[0], _ptr(occ), _ptr(out)))
+        return out
+
+
+@dataclass
+class SolveInfo:
+    nconv: int
+    restarts: int
+    matvecs: int
+    max_resid: float
+    seconds: float
+
+
+class Hamiltonian:
+    """H = J T + U V - mu N of one sector, assembled on the device once."""
+
+    def __init__(self, basis: Basis, neighbours):
+        self.basis = basis
+        off, flat = flatten_neighbours(neighbours)
+        if len(off) != basis.m + 1:
+            raise ValueError("neighbour lists must have one entry per site")
+        self._h = C.c_void_p()
+        _check(load().bh_hamiltonian_create(basis._h, _ptr(off), _ptr(flat), C.byref(self._h)))
+        nnz = C.c_int64()
+        _check(load().bh_hamiltonian_nnz(self._h, C.byref(nnz)))
+        self.nnz_offdiag = nnz.value
+        self.m, self.n, self.D = basis.m, basis.n, basis.D
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.bh_hamiltonian_destroy(self._h)
+            self._h = None
+
+    def csr_arrays(self, J: float, U: float, mu: float, order: int = ORDER_REFERENCE):
+        D, nz = self.D, self.nnz_offdiag + self.D
+        rp = np.zeros(D + 1, np.int64)
+        ci = np.zeros(nz, np.int32)
+        val = np.zeros(nz, np.float64)
+        _check(load().bh_hamiltonian_csr(self._h, order, J, U, mu, _ptr(rp), _ptr(ci), _ptr(val)))
+        return rp, ci, val
+
+    def csr(self, J: float, U: float, mu: float, order: int = ORDER_REFERENCE):
+        import scipy.sparse as sp
+
+        rp, ci, val = self.csr_arrays(J, U, mu, order)
+        return sp.csr_matrix((val, ci, rp), shape=(self.D, self.D))
+
+    def apply(self, x: np.ndarray, J: float, U: float, mu: float, order: int = ORDER_REFERENCE):
+        x = np.asarray(x, np.float64)
+        X = np.ascontiguousarray(x.reshape(self.D, -1))
+        Y = np.zeros_like(X)
+        _check(load().bh_hamiltonian_apply(self._h, order, J, U, mu, X.shape[1], _ptr(X), _ptr(Y)))
+        return Y.reshape(x.shape)
+
+    def eigsh(self, J: float, U: float, mu: float, nev: int = 10, vectors: bool = False,
+              order: int = ORDER_REFERENCE, **opt):
+        o = default_opts(nev=nev, order=order, **opt)
+        ev = np.zeros(nev)
+        rs = np.zeros(nev)
+        vec = np.zeros((nev, self.D)) if vectors else None
+        info = bh_solve_info()
+        _check(load().bh_eigsh(self._h, J, U, mu, C.byref(o), _ptr(ev), _ptr(rs), _ptr(vec),
+                               C.byref(info)))
+        return ev, rs, (None if vec is None else vec.T.copy()), _info(info)
+
+    def eigsh_batch(self, J, U, mu, nev: int = 10, **opt):
+        J = np.ascontiguousarray(J, np.float64)
+        S = len(J)
+        U = np.ascontiguousarray(np.broadcast_to(U, (S,)), np.float64)
+        mu = np.ascontiguousarray(np.broadcast_to(mu, (S,)), np.float64)
+        o = default_opts(nev=nev, **opt)
+        ev = np.zeros((S, nev))
+        rs = np.zeros((S, nev))
+        nc = np.zeros(S, np.int32)
+        info = bh_solve_info()
+        _check(load().bh_eigsh_batch(self._h, S, _ptr(J), _ptr(U), _ptr(mu), C.byref(o),
+                                     _ptr(ev), _ptr(rs), _ptr(nc), C.byref(info)))
+        return ev, rs, nc, _info(info)
+
+    def spdm(self, phi: np.ndarray, order: int = ORDER_REFERENCE) -> np.ndarray:
+        phi = np.ascontiguousarray(phi, np.float64)
+        rho = np.zeros(self.m * self.m)
+        _check(load().bh_spdm(self._h, order, _ptr(phi), _ptr(rho)))
+        return rho.reshape(self.m, self.m)
+
+
+def _info(i: bh_solve_info) -> SolveInfo:
+    return SolveInfo(i.nconv, i.restarts, i.matvecs, i.max_resid, i.seconds)
+
+
+# ---------------------------------------------------------------------------
+# BH namespace mirror (hamiltonian.hpp:33-112)
+# ---------------------------------------------------------------------------
+class BH:
+    @staticmethod
+    def dimension(m: int, n: int) -> int:
+        d = C.c_int64()
+        _check(load().bh_dimension(int(m), int(n), C.byref(d)))
+        return d.value
+
+    @staticmethod
+    def fixed_set_basis(m: int, n: int):
+        """(tags[D], basis[m, D]) in the reference's column order."""
+        b = Basis(m, n)
+        return b.copy()
+
+    @staticmethod
+    def fixed_bosons_hamiltonian(neighbours, basis, tags, m: int, n: int, J: float, U: float,
+                                 mu: float):
+        """One term of H, selected as the reference selects it (hamiltonian.cpp:238-256):
+        J T if J != 0, else U V, else -mu N; all zero prints an error and returns 0."""
+        import sys
+
+        import scipy.sparse as sp
+
+        eps = np.finfo(float).eps
+        D = BH.dimension(m, n)
+        if abs(J) > eps:
+            terms = (J, 0.0, 0.0)
+        elif abs(U) > eps:
+            terms = (0.0, U, 0.0)
+        elif abs(mu) > eps:
+            terms = (0.0, 0.0, mu)
+        else:
+            print("Error: At least one of the parameters J, U, mu must be different from zero.",
+                  file=sys.stderr)
+            return sp.csr_matrix((D, D))
+        h = Hamiltonian(Basis(m, n), neighbours)
+        H = h.csr(*terms)
+        if terms[0] != 0.0:
+            H.eliminate_zeros()  # hopping only: no diagonal entries, as fill_hopping
+            return H
+        # interaction / chemical term: one explicit entry per row, as fill_interaction
+        d = H.diagonal()
+        return sp.csr_matrix((d, np.arange(D, dtype=np.int32), np.arange(D + 1)), shape=(D, D))
+
+
+# ---------------------------------------------------------------------------
+# Op namespace mirror (operator.hpp:17-55)
+# ---------------------------------------------------------------------------
+class Op:
+    @staticmethod
+    def IRLM_eigen(O, nb_eigen: int, **opt):
+        """Lowest nb_eigen eigenpairs of the symmetric matrix O, returned as the
+        reference returns them: complex values ordered by descending |lambda|
+        and the matching eigenvectors as complex columns.  Raises
+        RuntimeError("Eigenvalue computation failed.") if not converged."""
+        import scipy.sparse as sp
+
+        A = sp.csr_matrix(O)
+        A.sort_indices()
+        D = A.shape[0]
+        rp = np.ascontiguousarray(A.indptr, np.int64)
+        ci = np.ascontiguousarray(A.indices, np.int32)
+        val = np.ascontiguousarray(A.data, np.float64)
+        o = default_opts(nev=nb_eigen, want_vectors=1, **opt)
+        ev = np.zeros(nb_eigen)
+        rs = np.zeros(nb_eigen)
+        vec = np.zeros((nb_eigen, D))
+        info = bh_solve_info()
+        rc = load().bh_eigsh_csr(D, _ptr(rp), _ptr(ci), _ptr(val), C.byref(o), _ptr(ev), _ptr(rs),
+                                 _ptr(vec), C.byref(info))
+        if rc == BH_ERR_NOCONV:
+            raise RuntimeError("Eigenvalue computation failed.")
+        _check(rc)
+        order = np.argsort(-np.abs(ev), kind="stable")
+        return ev[order].astype(complex), vec[order].T.astype(complex)
+
+
+# ---------------------------------------------------------------------------
+# Analysis namespace mirror (analysis.hpp)
+# ---------------------------------------------------------------------------
+class Analysis:
+    @staticmethod
+    def gap_ratios(eigenvalues, nb_eigen: int) -> np.ndarray:
+        ev = np.ascontiguousarray(np.real(np.asarray(eigenvalues))[:nb_eigen], np.float64)
+        r = np.zeros(max(nb_eigen - 2, 1))
+        mean = C.c_double()
+        _check(load().bh_gap_ratios(nb_eigen, _ptr(ev), _ptr(r), C.byref(mean)))
+        return r[: max(nb_eigen - 2, 0)]
+
+    @staticmethod
+    def coherence(spdm: np.ndarray) -> float:
+        s = np.asarray(spdm)
+        all_ = float(np.real(np.sum(s * s.T)))
+        diag = float(np.real(np.sum(np.diag(s) ** 2)))
+        return (all_ - diag) / all_
+
+    @staticmethod
+    def phase_map(m: int, n_lo: int, e0: np.ndarray, mu: np.ndarray):
+        """density, compressibility [nJ, nmu] from e0[nsec, nJ] (mu = 0 energies)."""
+        e0 = np.ascontiguousarray(e0, np.float64)
+        mu = np.ascontiguousarray(mu, np.float64)
+        nsec, nJ = e0.shape
+        dens = np.zeros((nJ, len(mu)))
+        kap = np.zeros((nJ, len(mu)))
+        _check(load().bh_phase_map(m, n_lo, nsec, nJ, _ptr(e0), len(mu), _ptr(mu), _ptr(dens),
+                                   _ptr(kap)))
+        return dens, kap

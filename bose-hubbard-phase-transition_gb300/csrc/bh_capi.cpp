@@ -1,0 +1,491 @@
+// bh_capi.cpp -- the C ABI (include/bh_gb300.h).  Every entry point converts
+// internal exceptions to a status code and keeps the message per thread.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "bh_internal.h"
+#include "bh_krylov.cuh"
+
+namespace bh {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+template <class F>
+static int guard(F&& f) {
+    try {
+        f();
+        g_last_error.clear();
+        return BH_OK;
+    } catch (const Error& e) {
+        g_last_error = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_last_error = "host allocation failed";
+        return BH_ERR_NOMEM;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return BH_ERR_ARG;
+    }
+}
+
+static std::vector<int32_t> host_copy_i32(const int32_t* d, int64_t n) {
+    std::vector<int32_t> h((size_t)n);
+    if (n) BH_CUDA(cudaMemcpy(h.data(), d, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    return h;
+}
+
+static void check_solver_opts(const bh_solver_opts* o) {
+    BH_REQUIRE(o != nullptr, "options pointer is null");
+    BH_REQUIRE(o->precision == BH_PREC_FP64 || o->precision == BH_PREC_MIXED, "unknown precision mode");
+    BH_REQUIRE(o->order == BH_ORDER_REFERENCE || o->order == BH_ORDER_LEX, "unknown vector order");
+    BH_REQUIRE(o->nev >= 1, "nb_eigen must be >= 1");
+}
+
+// fills the geometry of a request from the options and the dimension
+static SolveRequest make_request(const bh_solver_opts* o, int64_t D, int S) {
+    SolveRequest rq;
+    rq.S = S;
+    rq.nev = o->nev;
+    rq.precision = o->precision;
+    int p = o->block > 0 ? o->block : 2;
+    if ((int64_t)p * 2 > D) p = 1;
+    rq.p = p;
+    BH_REQUIRE(o->nev <= D - 2 || (D <= 2 && o->nev <= D), "nb_eigen must be <= dimension - 2");
+    int kmax = o->ncv > 0 ? o->ncv : std::max(3 * o->nev, o->nev + 6 * p);
+    kmax = (kmax + p - 1) / p * p;
+    if (kmax > D) kmax = (int)(D / p * p);
+    if (kmax < o->nev + p) {
+        // tiny dimension: the whole space
+        p = 1;
+        rq.p = 1;
+        kmax = (int)D;
+    }
+    rq.kmax = kmax;
+    rq.max_restarts = o->max_restarts > 0 ? o->max_restarts : 1000;
+    rq.tol = o->tol > 0.0 ? o->tol : (o->precision == BH_PREC_MIXED ? 3e-7 : 1e-10);
+    rq.seed = o->seed;
+    rq.want_vectors = o->want_vectors != 0;
+    return rq;
+}
+
+static void fill_info(bh_solve_info* info, const SolveResult& r, int nev, double secs) {
+    if (!info) return;
+    int mn = nev;
+    for (int c : r.nconv) mn = std::min(mn, c);
+    info->nconv = r.nconv.empty() ? 0 : mn;
+    info->restarts = r.restarts;
+    info->matvecs = r.matvecs;
+    double mx = 0.0;
+    for (double v : r.resid) mx = std::max(mx, v);
+    info->max_resid = mx;
+    info->seconds = secs;
+}
+
+}  // namespace bh
+
+using namespace bh;
+
+extern "C" {
+
+const char* bh_last_error(void) { return g_last_error.c_str(); }
+
+int bh_version(void) { return 10000; }
+
+// ---- lattices ----
+int bh_neighbours_chain(int m, int closed, int32_t* off, int32_t* nbr, int cap, int* count) {
+    return guard([&] {
+        BH_REQUIRE(off != nullptr, "offsets pointer is null");
+        flatten(chain_lists(m, closed != 0), off, nbr, cap, count);
+    });
+}
+int bh_neighbours_square(int m, int closed, int32_t* off, int32_t* nbr, int cap, int* count) {
+    return guard([&] {
+        BH_REQUIRE(off != nullptr, "offsets pointer is null");
+        flatten(square_lists(m, closed != 0), off, nbr, cap, count);
+    });
+}
+int bh_neighbours_cube(int m, int closed, int32_t* off, int32_t* nbr, int cap, int* count) {
+    return guard([&] {
+        BH_REQUIRE(off != nullptr, "offsets pointer is null");
+        flatten(cube_lists(m, closed != 0), off, nbr, cap, count);
+    });
+}
+
+// ---- basis ----
+int bh_dimension(int m, int n, int64_t* dim) {
+    return guard([&] {
+        BH_REQUIRE(dim != nullptr, "dim pointer is null");
+        BH_REQUIRE(m >= 1 && n >= 0, "m must be >= 1 and n >= 0");
+        const int64_t d = binomial64(m + n - 1, n);
+        BH_REQUIRE(d > 0, "dimension overflows 64 bits");
+        *dim = d;
+    });
+}
+
+int bh_basis_create(int m, int n, bh_basis** out) {
+    return guard([&] {
+        BH_REQUIRE(out != nullptr, "output pointer is null");
+        *out = nullptr;
+        BH_REQUIRE(m >= 1 && m <= kMaxSites, "m must be in [1, 25] (the reference's primes table)");
+        BH_REQUIRE(n >= 0 && n <= kMaxBosons, "n must be in [0, 60]");
+        const int64_t D = binomial64(m + n - 1, n);
+        BH_REQUIRE(D > 0 && D <= 2147483647LL, "dimension exceeds 2^31 - 1");
+        auto* b = new bh_basis();
+        try {
+            b->m = m;
+            b->n = n;
+            b->D = D;
+            BH_CUDA(cudaGetDevice(&b->device));
+            b->rt = make_rank_table(m, n);
+            Stream st;
+            basis_build(b, st);
+        } catch (...) {
+            delete b;
+            throw;
+        }
+        *out = b;
+    });
+}
+
+int bh_basis_destroy(bh_basis* b) {
+    return guard([&] { delete b; });
+}
+
+int bh_basis_info(const bh_basis* b, int* m, int* n, int64_t* dim) {
+    return guard([&] {
+        BH_REQUIRE(b != nullptr, "basis is null");
+        if (m) *m = b->m;
+        if (n) *n = b->n;
+        if (dim) *dim = b->D;
+    });
+}
+
+int bh_basis_copy(const bh_basis* b, double* tags, double* basis, int32_t* col_of_lex,
+                  int32_t* lex_of_col) {
+    return guard([&] {
+        BH_REQUIRE(b != nullptr, "basis is null");
+        const int64_t D = b->D;
+        Stream st;
+        if (tags || basis) {
+            DevBuf<double> dt(tags ? D : 1), db(basis ? D * b->m : 1);
+            basis_tags(b, tags ? dt.p : nullptr, basis ? db.p : nullptr, st);
+            if (tags) BH_CUDA(cudaMemcpy(tags, dt.p, D * sizeof(double), cudaMemcpyDeviceToHost));
+            if (basis) BH_CUDA(cudaMemcpy(basis, db.p, D * b->m * sizeof(double), cudaMemcpyDeviceToHost));
+        }
+        if (col_of_lex)
+            BH_CUDA(cudaMemcpy(col_of_lex, b->d_col_of_lex.p, D * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        if (lex_of_col)
+            BH_CUDA(cudaMemcpy(lex_of_col, b->d_lex_of_col.p, D * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    });
+}
+
+int bh_basis_index(const bh_basis* b, int64_t nq, const uint8_t* occ, int32_t* col) {
+    return guard([&] {
+        BH_REQUIRE(b != nullptr && (nq == 0 || (occ && col)), "null argument");
+        if (nq == 0) return;
+        Stream st;
+        DevBuf<uint8_t> dq((size_t)nq * b->m);
+        DevBuf<int32_t> dc(nq);
+        BH_CUDA(cudaMemcpyAsync(dq.p, occ, (size_t)nq * b->m, cudaMemcpyHostToDevice, st));
+        basis_index(b, nq, dq.p, dc.p, st);
+        BH_CUDA(cudaMemcpyAsync(col, dc.p, nq * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        BH_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+// ---- Hamiltonian ----
+int bh_hamiltonian_create(const bh_basis* b, const int32_t* nbr_off, const int32_t* nbr,
+                          bh_hamiltonian** out) {
+    return guard([&] {
+        BH_REQUIRE(b != nullptr && nbr_off != nullptr && out != nullptr, "null argument");
+        *out = nullptr;
+        const int m = b->m;
+        BH_REQUIRE(nbr_off[0] == 0, "neighbour offsets must start at 0");
+        for (int i = 0; i < m; ++i) BH_REQUIRE(nbr_off[i + 1] >= nbr_off[i], "neighbour offsets must be non-decreasing");
+        const int tot = nbr_off[m];
+        BH_REQUIRE(tot == 0 || nbr != nullptr, "neighbour list is null");
+        std::vector<int> cnt((size_t)m * m, 0);
+        for (int i = 0; i < m; ++i)
+            for (int k = nbr_off[i]; k < nbr_off[i + 1]; ++k) {
+                const int j = nbr[k];
+                BH_REQUIRE(j >= 0 && j < m, "neighbour index out of range");
+                BH_REQUIRE(j != i, "self-bond in the neighbour list");
+                cnt[(size_t)i * m + j] += 1;
+            }
+        for (int i = 0; i < m; ++i)
+            for (int j = 0; j < m; ++j)
+                BH_REQUIRE(cnt[(size_t)i * m + j] == cnt[(size_t)j * m + i], "neighbour lists must be symmetric");
+        auto* h = new bh_hamiltonian();
+        try {
+            h->basis = b;
+            h->m = m;
+            h->n = b->n;
+            h->D = b->D;
+            h->device = b->device;
+            h->h_nbr_off.assign(nbr_off, nbr_off + m + 1);
+            h->h_nbr.assign(nbr, nbr + tot);
+            Stream st;
+            hamiltonian_build(h, st);
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
+int bh_hamiltonian_destroy(bh_hamiltonian* h) {
+    return guard([&] { delete h; });
+}
+
+int bh_hamiltonian_nnz(const bh_hamiltonian* h, int64_t* nnz) {
+    return guard([&] {
+        BH_REQUIRE(h != nullptr && nnz != nullptr, "null argument");
+        *nnz = h->nnz;
+    });
+}
+
+int bh_hamiltonian_csr(const bh_hamiltonian* h, int order, double J, double U, double mu,
+                       int64_t* row_ptr, int32_t* col, double* val) {
+    return guard([&] {
+        BH_REQUIRE(h != nullptr && row_ptr && col && val, "null argument");
+        BH_REQUIRE(order == BH_ORDER_REFERENCE || order == BH_ORDER_LEX, "unknown order");
+        const int64_t D = h->D, nz = h->nnz + D;
+        Stream st;
+        DevBuf<int64_t> rp(D + 1);
+        DevBuf<int32_t> ci(nz);
+        DevBuf<double> v(nz);
+        hamiltonian_csr(h, order, J, U, mu, rp.p, ci.p, v.p, st);
+        BH_CUDA(cudaMemcpy(row_ptr, rp.p, (D + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost));
+        BH_CUDA(cudaMemcpy(col, ci.p, nz * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        BH_CUDA(cudaMemcpy(val, v.p, nz * sizeof(double), cudaMemcpyDeviceToHost));
+    });
+}
+
+static OpView<double> op64_of(const bh_hamiltonian* h) {
+    OpView<double> o;
+    o.rp = h->d_rp.p;
+    o.ci = h->d_ci.p;
+    o.tv = h->d_tv64.p;
+    o.vd = h->d_vd64.p;
+    o.D = h->D;
+    return o;
+}
+static OpView<float> op32_of(const bh_hamiltonian* h) {
+    OpView<float> o;
+    o.rp = h->d_rp.p;
+    o.ci = h->d_ci.p;
+    o.tv = h->d_tv32.p;
+    o.vd = h->d_vd32.p;
+    o.D = h->D;
+    return o;
+}
+
+int bh_hamiltonian_apply(const bh_hamiltonian* h, int order, double J, double U, double mu,
+                         int nvec, const double* x, double* y) {
+    return guard([&] {
+        BH_REQUIRE(h != nullptr && x && y && nvec >= 1, "null argument");
+        const int64_t D = h->D;
+        Stream st;
+        DevBuf<double> dx(D * nvec), dy(D * nvec), tmp(D * nvec), prm(3);
+        const double hp[3] = {J, U, -mu * (double)h->n};
+        BH_CUDA(cudaMemcpyAsync(prm.p, hp, sizeof hp, cudaMemcpyHostToDevice, st));
+        BH_CUDA(cudaMemcpyAsync(dx.p, x, D * nvec * sizeof(double), cudaMemcpyHostToDevice, st));
+        const bool ref = order == BH_ORDER_REFERENCE;
+        if (ref) gather_rows(D, nvec, h->basis->d_col_of_lex.p, dx.p, tmp.p, st);
+        apply_operator(op64_of(h), nvec, nvec, prm.p, ref ? tmp.p : dx.p, dy.p, st);
+        if (ref) gather_rows(D, nvec, h->basis->d_lex_of_col.p, dy.p, tmp.p, st);
+        BH_CUDA(cudaMemcpyAsync(y, ref ? tmp.p : dy.p, D * nvec * sizeof(double), cudaMemcpyDeviceToHost, st));
+        BH_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+// ---- eigensolver ----
+void bh_solver_opts_default(bh_solver_opts* o) {
+    if (!o) return;
+    o->nev = 10;
+    o->ncv = 0;
+    o->block = 0;
+    o->precision = BH_PREC_FP64;
+    o->max_restarts = 1000;
+    o->tol = 0.0;
+    o->seed = 0;
+    o->want_vectors = 0;
+    o->order = BH_ORDER_REFERENCE;
+}
+
+static void write_vectors(const bh_hamiltonian* h, const SolveResult& r, int S, int nev, int order,
+                          double* evecs) {
+    if (!evecs) return;
+    const int64_t D = h->D;
+    if (order == BH_ORDER_LEX) {
+        std::memcpy(evecs, r.vecs.data(), (size_t)S * nev * D * sizeof(double));
+        return;
+    }
+    const std::vector<int32_t> col = host_copy_i32(h->basis->d_col_of_lex.p, D);
+    for (int k = 0; k < S * nev; ++k)
+        for (int64_t rr = 0; rr < D; ++rr) evecs[(size_t)k * D + col[rr]] = r.vecs[(size_t)k * D + rr];
+}
+
+int bh_eigsh_batch(const bh_hamiltonian* h, int nsolve, const double* J, const double* U,
+                   const double* mu, const bh_solver_opts* o, double* evals, double* resid,
+                   int* nconv, bh_solve_info* info) {
+    return guard([&] {
+        const auto t0 = std::chrono::steady_clock::now();
+        BH_REQUIRE(h != nullptr && J && U && mu && evals, "null argument");
+        BH_REQUIRE(nsolve >= 1, "nsolve must be >= 1");
+        check_solver_opts(o);
+        SolveRequest rq = make_request(o, h->D, nsolve);
+        rq.want_vectors = false;
+        rq.d_perm = h->basis->d_col_of_lex.p;
+        rq.J.assign(J, J + nsolve);
+        rq.U.assign(U, U + nsolve);
+        rq.shift.resize(nsolve);
+        for (int s = 0; s < nsolve; ++s) rq.shift[s] = -mu[s] * (double)h->n;
+        Stream st;
+        SolveResult r = block_lanczos(op64_of(h), op32_of(h), rq, st);
+        std::memcpy(evals, r.evals.data(), r.evals.size() * sizeof(double));
+        if (resid) std::memcpy(resid, r.resid.data(), r.resid.size() * sizeof(double));
+        if (nconv) std::memcpy(nconv, r.nconv.data(), nsolve * sizeof(int));
+        const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        fill_info(info, r, o->nev, secs);
+    });
+}
+
+int bh_eigsh(const bh_hamiltonian* h, double J, double U, double mu, const bh_solver_opts* o,
+             double* evals, double* resid, double* evecs, bh_solve_info* info) {
+    return guard([&] {
+        const auto t0 = std::chrono::steady_clock::now();
+        BH_REQUIRE(h != nullptr && evals, "null argument");
+        check_solver_opts(o);
+        SolveRequest rq = make_request(o, h->D, 1);
+        rq.want_vectors = evecs != nullptr;
+        rq.d_perm = h->basis->d_col_of_lex.p;
+        rq.J = {J};
+        rq.U = {U};
+        rq.shift = {-mu * (double)h->n};
+        Stream st;
+        SolveResult r = block_lanczos(op64_of(h), op32_of(h), rq, st);
+        std::memcpy(evals, r.evals.data(), o->nev * sizeof(double));
+        if (resid) std::memcpy(resid, r.resid.data(), o->nev * sizeof(double));
+        write_vectors(h, r, 1, o->nev, o->order, evecs);
+        const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        fill_info(info, r, o->nev, secs);
+        if (r.nconv[0] < o->nev) throw Error(BH_ERR_NOCONV, "Eigenvalue computation failed.");
+    });
+}
+
+int bh_eigsh_csr(int64_t dim, const int64_t* row_ptr, const int32_t* col, const double* val,
+                 const bh_solver_opts* o, double* evals, double* resid, double* evecs,
+                 bh_solve_info* info) {
+    return guard([&] {
+        const auto t0 = std::chrono::steady_clock::now();
+        BH_REQUIRE(dim >= 1 && dim <= 2147483647LL, "dimension out of range");
+        BH_REQUIRE(row_ptr && col && val && evals, "null argument");
+        BH_REQUIRE(row_ptr[0] == 0, "row_ptr[0] must be 0");
+        check_solver_opts(o);
+        const int64_t nnz = row_ptr[dim];
+        for (int64_t r = 0; r < dim; ++r) BH_REQUIRE(row_ptr[r + 1] >= row_ptr[r], "row_ptr must be non-decreasing");
+        for (int64_t e = 0; e < nnz; ++e) BH_REQUIRE(col[e] >= 0 && col[e] < dim, "column index out of range");
+        Stream st;
+        DevBuf<int64_t> rp(dim + 1);
+        DevBuf<int32_t> ci(nnz);
+        DevBuf<double> v64(nnz);
+        DevBuf<float> v32;
+        std::vector<float> hv32;
+        BH_CUDA(cudaMemcpyAsync(rp.p, row_ptr, (dim + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+        if (nnz) {
+            BH_CUDA(cudaMemcpyAsync(ci.p, col, nnz * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+            BH_CUDA(cudaMemcpyAsync(v64.p, val, nnz * sizeof(double), cudaMemcpyHostToDevice, st));
+        }
+        if (o->precision == BH_PREC_MIXED) {
+            hv32.resize(nnz);
+            for (int64_t e = 0; e < nnz; ++e) hv32[e] = (float)val[e];
+            v32.alloc(nnz);
+            if (nnz) BH_CUDA(cudaMemcpyAsync(v32.p, hv32.data(), nnz * sizeof(float), cudaMemcpyHostToDevice, st));
+        }
+        OpView<double> a64;
+        a64.rp = rp.p;
+        a64.ci = ci.p;
+        a64.tv = v64.p;
+        a64.D = dim;
+        OpView<float> a32;
+        a32.rp = rp.p;
+        a32.ci = ci.p;
+        a32.tv = v32.p;
+        a32.D = dim;
+        SolveRequest rq = make_request(o, dim, 1);
+        rq.want_vectors = evecs != nullptr;
+        rq.J = {1.0};
+        rq.U = {0.0};
+        rq.shift = {0.0};
+        SolveResult r = block_lanczos(a64, a32, rq, st);
+        std::memcpy(evals, r.evals.data(), o->nev * sizeof(double));
+        if (resid) std::memcpy(resid, r.resid.data(), o->nev * sizeof(double));
+        if (evecs) std::memcpy(evecs, r.vecs.data(), (size_t)o->nev * dim * sizeof(double));
+        const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        fill_info(info, r, o->nev, secs);
+        if (r.nconv[0] < o->nev) throw Error(BH_ERR_NOCONV, "Eigenvalue computation failed.");
+    });
+}
+
+// ---- observables ----
+int bh_gap_ratios(int nev, const double* evals, double* ratios, double* mean) {
+    return guard([&] {
+        BH_REQUIRE(nev >= 0 && (nev == 0 || evals), "null argument");
+        std::vector<double> s(evals, evals + nev);
+        std::sort(s.begin(), s.end());
+        double sum = 0.0;
+        for (int i = 1; i + 1 < nev; ++i) {
+            const double up = s[i + 1] - s[i], dn = s[i] - s[i - 1];
+            const double mn = std::min(up, dn), mx = std::max(up, dn);
+            const double r = mx != 0.0 ? mn / mx : 0.0;
+            if (ratios) ratios[i - 1] = r;
+            sum += r;
+        }
+        if (mean) *mean = nev > 2 ? sum / (nev - 2) : 0.0;
+    });
+}
+
+int bh_spdm(const bh_hamiltonian* h, int order, const double* phi, double* rho) {
+    return guard([&] {
+        BH_REQUIRE(h != nullptr && phi && rho, "null argument");
+        const int64_t D = h->D;
+        Stream st;
+        DevBuf<double> dp(D), dl(D), dr((size_t)h->m * h->m);
+        BH_CUDA(cudaMemcpyAsync(dp.p, phi, D * sizeof(double), cudaMemcpyHostToDevice, st));
+        const double* lex = dp.p;
+        if (order == BH_ORDER_REFERENCE) {
+            gather_rows(D, 1, h->basis->d_col_of_lex.p, dp.p, dl.p, st);
+            lex = dl.p;
+        }
+        spdm_device(h, lex, dr.p, st);
+        BH_CUDA(cudaMemcpyAsync(rho, dr.p, (size_t)h->m * h->m * sizeof(double), cudaMemcpyDeviceToHost, st));
+        BH_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+int bh_phase_map(int m, int n_lo, int nsec, int nJ, const double* e0, int nmu, const double* mu,
+                 double* density, double* compressibility) {
+    return guard([&] {
+        BH_REQUIRE(m >= 1 && nsec >= 1 && nJ >= 1 && nmu >= 1, "empty grid");
+        BH_REQUIRE(e0 && mu && density && compressibility, "null argument");
+        Stream st;
+        DevBuf<double> de((size_t)nsec * nJ), dm(nmu), dd((size_t)nJ * nmu), dk((size_t)nJ * nmu);
+        BH_CUDA(cudaMemcpyAsync(de.p, e0, (size_t)nsec * nJ * sizeof(double), cudaMemcpyHostToDevice, st));
+        BH_CUDA(cudaMemcpyAsync(dm.p, mu, nmu * sizeof(double), cudaMemcpyHostToDevice, st));
+        phase_map_device(m, n_lo, nsec, nJ, de.p, nmu, dm.p, dd.p, dk.p, st);
+        BH_CUDA(cudaMemcpyAsync(density, dd.p, (size_t)nJ * nmu * sizeof(double), cudaMemcpyDeviceToHost, st));
+        BH_CUDA(cudaMemcpyAsync(compressibility, dk.p, (size_t)nJ * nmu * sizeof(double), cudaMemcpyDeviceToHost, st));
+        BH_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,165 @@
+// bh_internal.h -- internal declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/bh_gb300.h"
+
+namespace bh {
+
+// ---------------------------------------------------------------------------
+// errors: internal code throws bh::Error; the C ABI converts it to a status
+// code and stores the message for bh_last_error().
+// ---------------------------------------------------------------------------
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void set_last_error(const std::string& msg);
+
+#define BH_CUDA(call)                                                                    \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess)                                                           \
+            throw ::bh::Error(BH_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define BH_REQUIRE(cond, msg)                                  \
+    do {                                                       \
+        if (!(cond)) throw ::bh::Error(BH_ERR_ARG, (msg));     \
+    } while (0)
+
+// Owning device buffer.
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    explicit DevBuf(size_t count) { alloc(count); }
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DevBuf& operator=(DevBuf&& o) noexcept {
+        if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void alloc(size_t count) {
+        release();
+        if (count == 0) count = 1;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            (void)cudaGetLastError();
+            throw Error(BH_ERR_NOMEM, "cudaMalloc of " + std::to_string(count * sizeof(T)) +
+                                          " bytes failed: " + cudaGetErrorString(e));
+        }
+        n = count;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+// Stream owned by one library call (calls are re-entrant across threads).
+struct Stream {
+    cudaStream_t s = nullptr;
+    Stream() { BH_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)); }
+    ~Stream() { if (s) cudaStreamDestroy(s); }
+    operator cudaStream_t() const { return s; }
+};
+
+int sm_count();
+
+// ---------------------------------------------------------------------------
+// Fock basis.  States are identified by their lexicographic index r (the
+// enumeration order of the reference's init_lexicographic).  rank table
+// RT[i][s] = C(s + m - i - 2, m - i - 1), i in [0, m-2], s in [0, n]:
+//   r = sum_i RT[i][s_i],  s_i = sum_{j > i} n_j.
+// ---------------------------------------------------------------------------
+constexpr int kMaxSites = 25;   // primes table of the reference (hamiltonian.cpp:144)
+constexpr int kMaxBosons = 60;  // occupations stored as uint8, keys must fit 128 bits
+
+struct RankTable {
+    int m = 0, n = 0;
+    std::vector<uint32_t> host;  // (m-1) x (n+1)
+};
+RankTable make_rank_table(int m, int n);
+int64_t binomial64(int n, int k);
+
+}  // namespace bh
+
+struct bh_basis {
+    int m = 0, n = 0;
+    int64_t D = 0;
+    int device = 0;
+    bh::RankTable rt;
+    bh::DevBuf<uint32_t> d_rt;          // rank table
+    bh::DevBuf<int32_t> d_col_of_lex;   // lexicographic -> reference column
+    bh::DevBuf<int32_t> d_lex_of_col;   // reference column -> lexicographic
+};
+
+struct bh_hamiltonian {
+    const bh_basis* basis = nullptr;
+    int m = 0, n = 0;
+    int64_t D = 0;
+    int64_t nnz = 0;  // off-diagonal entries of T
+    int device = 0;
+    std::vector<int32_t> h_nbr_off, h_nbr;
+    bh::DevBuf<int32_t> d_nbr_off, d_nbr;
+    // T in lexicographic order (rows and columns), values of T (J = 1)
+    bh::DevBuf<int64_t> d_rp;
+    bh::DevBuf<int32_t> d_ci;
+    bh::DevBuf<double> d_tv64;
+    bh::DevBuf<float> d_tv32;
+    // diagonal V in lexicographic order
+    bh::DevBuf<double> d_vd64;
+    bh::DevBuf<float> d_vd32;
+};
+
+namespace bh {
+
+// ---- launchers (bh_basis.cu) ----
+void basis_build(bh_basis* b, cudaStream_t st);
+void basis_tags(const bh_basis* b, double* d_tags, double* d_occ_cols, cudaStream_t st);
+void basis_index(const bh_basis* b, int64_t nq, const uint8_t* d_occ, int32_t* d_col,
+                 cudaStream_t st);
+void scan_exclusive_i64(const int64_t* d_in, int64_t* d_out, int64_t n, cudaStream_t st);
+
+// ---- launchers (bh_hamiltonian.cu) ----
+void hamiltonian_build(bh_hamiltonian* h, cudaStream_t st);
+// CSR of H = J T + U V - mu N with diagonal entries, rows/cols in `order`.
+void hamiltonian_csr(const bh_hamiltonian* h, int order, double J, double U, double mu,
+                     int64_t* d_rp, int32_t* d_ci, double* d_val, cudaStream_t st);
+void spdm_device(const bh_hamiltonian* h, const double* d_phi_lex, double* d_rho,
+                 cudaStream_t st);
+// out[r][0..ncols) = in[map[r]][0..ncols)  (double)
+void gather_rows(int64_t D, int ncols, const int32_t* d_map, const double* d_in, double* d_out,
+                 cudaStream_t st);
+// density / compressibility maps from sector ground energies (device)
+void phase_map_device(int m, int n_lo, int nsec, int nJ, const double* d_e0, int nmu,
+                      const double* d_mu, double* d_density, double* d_kappa, cudaStream_t st);
+
+// ---- lattices (bh_lattice.cpp) ----
+using Lists = std::vector<std::vector<int32_t>>;
+Lists chain_lists(int m, bool closed);
+Lists square_lists(int m, bool closed);
+Lists cube_lists(int m, bool closed);
+void flatten(const Lists& nb, int32_t* off, int32_t* out, int cap, int* count);
+
+// ---- host dense symmetric eigensolver (bh_symeig.cpp) ----
+// a: n x n column-major symmetric, overwritten with eigenvectors (columns);
+// w: eigenvalues ascending.  Returns false if the iteration did not converge.
+bool symeig(int n, double* a, double* w);
+
+}  // namespace bh

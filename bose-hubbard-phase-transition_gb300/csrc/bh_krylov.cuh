@@ -1,0 +1,54 @@
+// bh_krylov.cuh -- block thick-restart Lanczos on the device (declarations).
+#pragma once
+
+#include "bh_internal.h"
+
+namespace bh {
+
+// Sparse operator  y_t = J_s (T x)_t + (U_s vd + shift_s) x_t  for column t of
+// solve s = t / group.  vd may be null (plain CSR of a full matrix, U = 0).
+template <class T>
+struct OpView {
+    const int64_t* rp = nullptr;
+    const int32_t* ci = nullptr;
+    const T* tv = nullptr;
+    const T* vd = nullptr;
+    int64_t D = 0;
+};
+
+struct SolveRequest {
+    int S = 1;                 // solves in the batch (share the operator pattern)
+    int nev = 10;
+    int p = 2;                 // block size
+    int kmax = 0;              // basis size (multiple of p)
+    int max_restarts = 1000;
+    double tol = 1e-10;
+    int precision = BH_PREC_FP64;
+    uint64_t seed = 0;
+    const int32_t* d_perm = nullptr;  // start-vector index map (row -> reference index)
+    std::vector<double> J, U, shift;  // per solve
+    bool want_vectors = false;
+};
+
+struct SolveResult {
+    std::vector<double> evals;   // S x nev, ascending
+    std::vector<double> resid;   // S x nev, relative residual norms
+    std::vector<int> nconv;      // S
+    std::vector<int> conv_at;    // S: restart count at which the solve converged (-1: never)
+    std::vector<double> scale;   // S: spectral radius estimate (largest |Ritz value|)
+    std::vector<double> vecs;    // S x nev x D (lexicographic/operator order), if requested
+    int restarts = 0;
+    int64_t matvecs = 0;
+    int64_t launches = 0;        // kernels launched by the solve
+    bool breakdown = false;
+};
+
+// Y = H X (FP64) for ncols columns, solve of column t = t / group, prm[3 s..] = (J, U, shift).
+void apply_operator(const OpView<double>& op, int ncols, int group, const double* d_prm,
+                    const double* d_X, double* d_Y, cudaStream_t st);
+
+// op64 must be set; op32 must be set for BH_PREC_MIXED (same pattern).
+SolveResult block_lanczos(const OpView<double>& op64, const OpView<float>& op32,
+                          const SolveRequest& rq, cudaStream_t st);
+
+}  // namespace bh

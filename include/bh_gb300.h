@@ -1,0 +1,196 @@
+/*
+ * bh_gb300.h -- C ABI of the GB300-native exact-diagonalisation engine for the
+ * Bose-Hubbard model.
+ *
+ * Every entry point is a plain C function over plain pointers and sizes.  The
+ * library owns device memory behind opaque handles (bh_basis, bh_hamiltonian)
+ * and writes results into caller-allocated HOST buffers.  Every function
+ * returns a status code (BH_OK on success); bh_last_error() gives the message
+ * of the last failure on the calling thread.
+ *
+ * The comment above each declaration names the reference interface it
+ * replaces (Maximilien-Hantonne/Bose-Hubbard-Phase-Transition, file:line).
+ *
+ * Conventions
+ *  - Hamiltonian  H = J T + U V - mu N,  T = -sum_i sum_{j in nbr(i)} b+_i b_j,
+ *    V = 1/2 sum_i n_i (n_i - 1), N = sum_i n_i (= n in a fixed-n sector).
+ *  - "reference order" is the column order of BH::fixed_set_basis
+ *    (hamiltonian.cpp:143-149); "lexicographic order" is the order of
+ *    BH::init_lexicographic (hamiltonian.cpp:75-85).
+ *  - Neighbour lists are CSR-like: nbr[off[i] .. off[i+1]) are the neighbours
+ *    of site i, as std::vector<std::vector<int>> Neighbours::getNeighbours()
+ *    (neighbours.cpp:126-128) holds them.
+ */
+#ifndef BH_GB300_H
+#define BH_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference throws; see bh_reference_api.hpp) ---- */
+#define BH_OK 0
+#define BH_ERR_ARG 1       /* invalid argument (std::invalid_argument)            */
+#define BH_ERR_NOCONV 2    /* not converged ("Eigenvalue computation failed.")    */
+#define BH_ERR_BREAKDOWN 3 /* Krylov breakdown that could not be recovered        */
+#define BH_ERR_TIMEOUT 4   /* a bounded device wait ran out                        */
+#define BH_ERR_CUDA 5      /* CUDA runtime error                                   */
+#define BH_ERR_NOMEM 6     /* device or host allocation failed                     */
+
+#define BH_ORDER_REFERENCE 0
+#define BH_ORDER_LEX 1
+
+#define BH_PREC_FP64 0  /* vectors, SpMV and recurrence in FP64 (the plain method) */
+#define BH_PREC_MIXED 1 /* FP32 vectors/SpMM, FP64 coefficients + FP64 refinement  */
+
+typedef struct bh_basis bh_basis;
+typedef struct bh_hamiltonian bh_hamiltonian;
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* bh_last_error(void);
+/* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
+int bh_version(void);
+
+/* ---------------------------------------------------------------------- */
+/* Lattice (host)                                                          */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces Neighbours::chain_neighbours (neighbours.cpp:21-34): 1D chain,
+ * periodic when closed != 0.  Writes off[m+1] and up to cap entries of nbr;
+ * *count receives the total number of entries. */
+int bh_neighbours_chain(int m, int closed, int32_t* off, int32_t* nbr, int cap, int* count);
+/* Replaces Neighbours::square_neighbours (neighbours.cpp:40-71) with the
+ * lists that function intends (the reference fills a shadowing local and
+ * returns empty lists).  m must be a perfect square (else BH_ERR_ARG, the
+ * reference's std::invalid_argument). */
+int bh_neighbours_square(int m, int closed, int32_t* off, int32_t* nbr, int cap, int* count);
+/* Replaces Neighbours::cube_neighbours (neighbours.cpp:77-120), as above;
+ * m must be a perfect cube. */
+int bh_neighbours_cube(int m, int closed, int32_t* off, int32_t* nbr, int cap, int* count);
+
+/* ---------------------------------------------------------------------- */
+/* Fock basis                                                              */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces BH::dimension / BH::binomial (hamiltonian.cpp:39-54). */
+int bh_dimension(int m, int n, int64_t* dim);
+
+/* Replaces BH::fixed_set_basis (hamiltonian.cpp:143-149): builds the basis
+ * on the device (combinadic unranking, exact 128-bit prime-product keys,
+ * device radix sort).  m <= 25 (the reference's primes table). */
+int bh_basis_create(int m, int n, bh_basis** out);
+int bh_basis_destroy(bh_basis* b);
+int bh_basis_info(const bh_basis* b, int* m, int* n, int64_t* dim);
+/* Copies the basis out in the reference's representation.  Any pointer may
+ * be NULL.  tags[D] and basis[m*D] (column-major, column c = occupation of
+ * the state at reference column c) equal the pair fixed_set_basis returns;
+ * col_of_lex[D] maps lexicographic index -> reference column and
+ * lex_of_col[D] the inverse. */
+int bh_basis_copy(const bh_basis* b, double* tags, double* basis, int32_t* col_of_lex,
+                  int32_t* lex_of_col);
+/* Replaces BH::search_tag on the exact state (hamiltonian.cpp:126-140):
+ * reference column of each of nq occupations occ[nq*m] (uint8, row-major);
+ * -1 where the occupation is not in the sector. */
+int bh_basis_index(const bh_basis* b, int64_t nq, const uint8_t* occ, int32_t* col);
+
+/* ---------------------------------------------------------------------- */
+/* Hamiltonian                                                             */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces BH::fixed_bosons_hamiltonian / fill_hopping / fill_interaction /
+ * fill_chemical (hamiltonian.cpp:170-256): assembles the hopping term T
+ * (warp per row CSR, sorted columns, duplicate bonds merged) and the
+ * diagonal V on the device, once, for all (J, U, mu).  The neighbour lists
+ * must be symmetric and free of self-bonds. */
+int bh_hamiltonian_create(const bh_basis* b, const int32_t* nbr_off, const int32_t* nbr,
+                          bh_hamiltonian** out);
+int bh_hamiltonian_destroy(bh_hamiltonian* h);
+/* Number of stored off-diagonal entries of T. */
+int bh_hamiltonian_nnz(const bh_hamiltonian* h, int64_t* nnz_offdiag);
+/* Writes H = J T + U V - mu N as CSR into host buffers, rows and columns in
+ * `order`, with one (explicit, possibly zero) diagonal entry per row and
+ * sorted columns: row_ptr[D+1], col[nnz_offdiag + D], val[nnz_offdiag + D]. */
+int bh_hamiltonian_csr(const bh_hamiltonian* h, int order, double J, double U, double mu,
+                       int64_t* row_ptr, int32_t* col, double* val);
+/* y = H x for nvec vectors (x, y: host, row-major [D][nvec], `order`). */
+int bh_hamiltonian_apply(const bh_hamiltonian* h, int order, double J, double U, double mu,
+                         int nvec, const double* x, double* y);
+
+/* ---------------------------------------------------------------------- */
+/* Eigensolver                                                             */
+/* ---------------------------------------------------------------------- */
+
+typedef struct bh_solver_opts {
+    int nev;          /* wanted lowest eigenvalues (the reference's nb_eigen)         */
+    int ncv;          /* max Krylov basis size per solve; 0 = automatic               */
+    int block;        /* block size p (>= degeneracy to resolve); 0 = automatic       */
+    int precision;    /* BH_PREC_FP64 or BH_PREC_MIXED                                 */
+    int max_restarts; /* restart cap (the reference's maxit = 1000)                    */
+    double tol;       /* relative residual tolerance; 0 = 1e-10 (FP64) / auto (mixed) */
+    uint64_t seed;    /* start block seed (Spectra SimpleRandom seed; 0 == 1)          */
+    int want_vectors; /* nonzero: return Ritz vectors                                  */
+    int order;        /* order of returned vectors: BH_ORDER_REFERENCE or BH_ORDER_LEX */
+} bh_solver_opts;
+
+typedef struct bh_solve_info {
+    int nconv;         /* converged eigenvalues (per solve, minimum over a batch) */
+    int restarts;      /* thick restarts performed                                */
+    int64_t matvecs;   /* H x products per solve                                  */
+    double max_resid;  /* max relative residual of the returned pairs             */
+    double seconds;    /* wall time of the call                                   */
+} bh_solve_info;
+
+void bh_solver_opts_default(bh_solver_opts* o);
+
+/* Replaces Op::IRLM_eigen (operator.cpp:22-33) for one (J, U, mu) point of a
+ * built Hamiltonian: the nev lowest eigenvalues, ascending, in evals[nev];
+ * per-pair relative residuals in resid[nev] (may be NULL); Ritz vectors in
+ * evecs[nev*D] (row i = vector i, in opts->order; may be NULL). */
+int bh_eigsh(const bh_hamiltonian* h, double J, double U, double mu, const bh_solver_opts* o,
+             double* evals, double* resid, double* evecs, bh_solve_info* info);
+
+/* Replaces Op::IRLM_eigen (operator.cpp:22-33) on an arbitrary symmetric
+ * matrix given as CSR in host memory (Eigen's compressed storage of a
+ * symmetric matrix can be passed as is).  Same outputs as bh_eigsh. */
+int bh_eigsh_csr(int64_t dim, const int64_t* row_ptr, const int32_t* col, const double* val,
+                 const bh_solver_opts* o, double* evals, double* resid, double* evecs,
+                 bh_solve_info* info);
+
+/* Replaces the OpenMP grid loop of Analysis::calculate_and_save
+ * (analysis.cpp:302-314): nsolve (J, U, mu) points of one Hamiltonian solved
+ * together as one batch (shared-pattern SpMM, device-resident Krylov loop).
+ * evals[nsolve*nev] ascending per solve; resid[nsolve*nev] (may be NULL);
+ * nconv[nsolve] (may be NULL). */
+int bh_eigsh_batch(const bh_hamiltonian* h, int nsolve, const double* J, const double* U,
+                   const double* mu, const bh_solver_opts* o, double* evals, double* resid,
+                   int* nconv, bh_solve_info* info);
+
+/* ---------------------------------------------------------------------- */
+/* Observables                                                             */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces Analysis::gap_ratios (analysis.cpp:433-454): ratios[nev-2] of the
+ * sorted values; returns the mean in *mean. */
+int bh_gap_ratios(int nev, const double* evals, double* ratios, double* mean);
+
+/* Replaces Analysis::SPDM / braket (analysis.cpp:497-528, 562-594) with the
+ * single-particle density matrix they intend: rho[m*m] (row-major) =
+ * <phi| b+_i b_j |phi> for a real vector phi[D] given in `order`. */
+int bh_spdm(const bh_hamiltonian* h, int order, const double* phi, double* rho);
+
+/* Phase-map composition over particle-number sectors (the exact path's
+ * boson density / compressibility, with mu applied as the -mu n shift):
+ * e0[nsec*nJ] ground energies at mu = 0 for sectors n_lo..n_lo+nsec-1,
+ * mu[nmu]; outputs density[nJ*nmu] = nbest / m with
+ * nbest = argmin_n E0(n) - mu n, and compressibility[nJ*nmu] = d density / d mu
+ * (central differences, one-sided at the ends of the mu grid). */
+int bh_phase_map(int m, int n_lo, int nsec, int nJ, const double* e0, int nmu, const double* mu,
+                 double* density, double* compressibility);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BH_GB300_H */

@@ -1,0 +1,173 @@
+"""Generate the golden fixtures of tests/golden/ from the reference itself.
+
+Runs the reference's own exact-path code, compiled from its sources by
+oracle/Makefile into oracle/_ref/libbhref.so:
+  - BH::fixed_set_basis / init_lexicographic (hamiltonian.cpp:60-149):
+    reference column order and tags (tags recorded bit-exactly as hex);
+  - Neighbours (neighbours.cpp:21-120): the lists the reference returns;
+  - Op::IRLM_eigen (operator.cpp:22-33, Spectra GenEigsSolver) and
+    Op::exact_eigen on the Bose-Hubbard Hamiltonian with the physics of the
+    reference's model definition (H = -J sum b+b + U/2 sum n(n-1) - mu sum n),
+    assembled in the reference's column order by the CPU oracle (the
+    reference's own builder is not a valid Hamiltonian: it loops over
+    neighbour slots and reads out of bounds);
+  - Analysis::gap_ratios and Analysis::coherence.
+Usage:  python tests/golden/make_golden.py [--quick]
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import hashlib
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import oracle as orc  # noqa: E402
+
+REF_TREE = "/root/reference"
+
+
+def hexs(a):
+    return [float(x).hex() for x in a]
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def ref_order_from_reference(ref, m, n):
+    """col_of_lex from the reference's own basis matrix."""
+    tags, basis = ref.fixed_set_basis(m, n)  # basis[c] = occupation at column c
+    lex = ref.init_lexicographic(m, n)
+    index = {tuple(row.astype(int)): i for i, row in enumerate(lex)}
+    lex_of_col = np.array([index[tuple(row.astype(int))] for row in basis], np.int32)
+    col_of_lex = np.empty_like(lex_of_col)
+    col_of_lex[lex_of_col] = np.arange(len(lex_of_col), dtype=np.int32)
+    return tags, col_of_lex, lex_of_col
+
+
+def chain(m):
+    off = np.zeros(m + 1, np.int32)
+    nb = []
+    lists = [[] for _ in range(m)]
+    for i in range(m):
+        if i > 0:
+            lists[i].append(i - 1)
+        if i < m - 1:
+            lists[i].append(i + 1)
+    lists[0].append(m - 1)
+    lists[m - 1].append(0)
+    for i, l in enumerate(lists):
+        nb += l
+        off[i + 1] = len(nb)
+    return off, np.array(nb, np.int32)
+
+
+def hamiltonian_ref_order(o, m, n, J, U, mu, nbr=None):
+    occ = o.lex_states(m, n)
+    col_of_lex, lex_of_col = o.reference_order(occ)
+    off, nb = nbr if nbr is not None else chain(m)
+    rp, ci, tv = o.build_T(occ, off, nb, lex_of_col, col_of_lex)
+    vd = o.diag_V(occ, lex_of_col)
+    return o.full_csr(rp, ci, tv, vd, n, J, U, mu)
+
+
+def main(quick: bool):
+    orc.build()
+    if orc.build_ref(REF_TREE) is None:
+        raise SystemExit("reference tree not available")
+    o = orc.Oracle()
+    ref = orc.Reference()
+    out = {"generator": "tests/golden/make_golden.py", "reference": "Maximilien-Hantonne/Bose-Hubbard-Phase-Transition"}
+
+    # ---- basis ----
+    small = [(1, 0), (1, 3), (2, 0), (2, 3), (3, 3), (4, 4), (5, 3), (3, 5), (6, 6), (4, 7), (8, 8)]
+    hashed = [(10, 10), (12, 6), (7, 9), (10, 8), (10, 12)]
+    basis = {}
+    for m, n in small + hashed:
+        tags, col_of_lex, lex_of_col = ref_order_from_reference(ref, m, n)
+        rec = {"m": m, "n": n, "D": int(len(tags)),
+               "col_of_lex_sha256": sha(col_of_lex.astype("<i4")),
+               "tags_sha256": sha(tags.astype("<f8"))}
+        if (m, n) in small:
+            rec["col_of_lex"] = col_of_lex.tolist()
+            rec["tags_hex"] = hexs(tags)
+        basis[f"{m},{n}"] = rec
+    out["basis"] = basis
+
+    # ---- neighbours as the reference returns them ----
+    nbrs = {}
+    for kind, name, ms in [(1, "chain", [2, 3, 4, 5, 8]), (2, "square", [4, 9, 16]), (3, "cube", [8, 27])]:
+        for m in ms:
+            for closed in (True, False):
+                off, nb = ref.neighbours(kind, m, closed)
+                nbrs[f"{name},{m},{int(closed)}"] = {"off": off.tolist(), "nbr": nb.tolist()}
+    out["neighbours"] = nbrs
+
+    # ---- eigenvalues: reference IRLM on the model Hamiltonian ----
+    cases = [
+        ("m8n8", 8, 8, 0.1, 1.0, 0.5, 10),
+        ("m6n6", 6, 6, 0.1, 1.0, 0.5, 6),
+        ("m5n5_J0.2", 5, 5, 0.2, 1.0, 0.0, 6),
+        ("m6n4_J0.3", 6, 4, 0.3, 1.0, 0.25, 8),
+        ("m10n8", 10, 8, 0.15, 1.0, 0.0, 10),
+    ]
+    if not quick:
+        cases += [("m10n10", 10, 10, 0.15, 1.0, 0.0, 10)]
+    # batched grid points: m = 10, sectors 8..12, J_b = 0.3 (b + 1) / 64
+    grid_b = [3, 15, 31, 47, 63] if not quick else [31]
+    grid_n = [8, 9, 10, 11, 12] if not quick else [8, 9]
+    for n in grid_n:
+        for b in grid_b:
+            cases.append((f"grid_n{n}_b{b}", 10, n, 0.3 * (b + 1) / 64, 1.0, 0.0, 10))
+
+    def run(case):
+        name, m, n, J, U, mu, nev = case
+        H = hamiltonian_ref_order(o, m, n, J, U, mu)
+        t0 = time.time()
+        try:
+            re, im = ref.irlm(H, nev)
+            ok = True
+        except RuntimeError:
+            re, im, ok = np.zeros(0), np.zeros(0), False
+        dt = time.time() - t0
+        return name, {"m": m, "n": n, "J": J, "U": U, "mu": mu, "nev": nev, "converged": ok,
+                      "evals_reference_order": re.tolist(), "imag_max": float(np.abs(im).max()) if len(im) else 0.0,
+                      "evals_sorted": sorted(re.tolist()), "seconds": dt, "nnz": int(H.nnz)}
+
+    eig = {}
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        for name, rec in ex.map(run, cases):
+            eig[name] = rec
+            print(f"{name}: conv={rec['converged']} t={rec['seconds']:.1f}s E0={rec['evals_sorted'][:1]}", flush=True)
+    out["irlm"] = eig
+
+    # ---- dense spectra (Op::exact_eigen) for small sectors ----
+    dense = {}
+    for m, n, J, U, mu in [(4, 4, 0.1, 1.0, 0.5), (5, 3, 0.3, 1.0, 0.2), (3, 3, 0.0, 1.0, 0.5), (4, 3, 0.25, 0.0, 0.0)]:
+        H = hamiltonian_ref_order(o, m, n, J, U, mu)
+        dense[f"{m},{n},{J},{U},{mu}"] = ref.exact_eigen(H).tolist()
+    out["exact_eigen"] = dense
+
+    # ---- analysis helpers ----
+    ev = np.array(eig["m8n8"]["evals_reference_order"])
+    out["gap_ratios_m8n8"] = ref.gap_ratios(ev).tolist()
+    rng = np.random.RandomState(7)
+    rho = rng.rand(5, 5)
+    rho = rho + rho.T
+    out["coherence"] = {"rho": rho.tolist(), "value": ref.coherence(rho)}
+
+    path = os.path.join(HERE, "reference_golden.json")
+    with open(path, "w") as f:
+        json.dump(out, f, indent=1)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__":
+    main("--quick" in sys.argv)

@@ -1,0 +1,108 @@
+"""GPU: eigensolver parity.
+
+FP64 plain method: eigenvalues within 1e-10 relative of the reference's Spectra
+IRLM results (golden), including degenerate copies.  Mixed precision: within
+1e-8 relative of the FP64 results."""
+import numpy as np
+import pytest
+
+from conftest import chain_lists, oracle_H
+
+pytestmark = pytest.mark.gpu
+
+RTOL_FP64 = 1e-10
+RTOL_MIXED = 1e-8
+
+
+def _rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300))
+
+
+@pytest.mark.parametrize("name", ["m8n8", "m6n6", "m5n5_J0.2", "m6n4_J0.3", "m10n8"])
+def test_fp64_matches_reference_irlm(pkg, golden, name):
+    rec = golden["irlm"][name]
+    m, n = rec["m"], rec["n"]
+    h = pkg.Hamiltonian(pkg.Basis(m, n), chain_lists(m))
+    ev, rs, _, info = h.eigsh(rec["J"], rec["U"], rec["mu"], nev=rec["nev"])
+    assert _rel(ev, rec["evals_sorted"]) < RTOL_FP64
+    assert np.all(rs < 1e-9)
+    assert info.nconv == rec["nev"]
+
+
+def test_m8_known_answers(pkg):
+    h = pkg.Hamiltonian(pkg.Basis(8, 8), chain_lists(8))
+    ev, _, _, _ = h.eigsh(0.1, 1.0, 0.5, nev=10)
+    assert abs(ev[0] - (-4.317353604401086)) < 1e-12
+    # degenerate pairs are resolved with multiplicity
+    assert abs(ev[2] - ev[3]) < 1e-11 and abs(ev[2] - (-3.7235662)) < 1e-7
+
+
+def test_analytic_limits(pkg, orc):
+    m, n = 8, 6
+    h = pkg.Hamiltonian(pkg.Basis(m, n), chain_lists(m))
+    # U = 0: free bosons, E0 = -2 J n
+    J = 0.4
+    ev, _, _, _ = h.eigsh(J, 0.0, 0.0, nev=4)
+    assert abs(ev[0] + 2 * J * n) < 1e-10
+    # sums of single-particle levels -2J cos(2 pi k / m): first excitation
+    eps = np.sort(-2 * J * np.cos(2 * np.pi * np.arange(m) / m))
+    assert abs(ev[1] - ((n - 1) * eps[0] + eps[1])) < 1e-10
+    # J -> tiny: diagonal U/2 sum n(n-1) - mu n; lowest = distribute evenly
+    ev, _, _, _ = h.eigsh(1e-9, 1.0, 0.3, nev=2)
+    assert abs(ev[0] - (0.0 - 0.3 * n)) < 1e-6
+
+
+def test_irlm_eigen_dropin_on_generic_matrix(pkg, golden, orc):
+    rec = golden["irlm"]["m8n8"]
+    _, _, _, rp, ci, tv, vd = oracle_H(orc, 8, 8, chain_lists(8))
+    H = orc.full_csr(rp, ci, tv, vd, 8, rec["J"], rec["U"], rec["mu"])
+    vals, vecs = pkg.Op.IRLM_eigen(H, 10)
+    assert vals.dtype == complex and vecs.shape == (H.shape[0], 10)
+    # reference ordering: descending magnitude
+    np.testing.assert_allclose(vals.real, rec["evals_reference_order"], rtol=RTOL_FP64)
+    R = H @ vecs.real - vecs.real * vals.real
+    assert np.linalg.norm(R, axis=0).max() < 1e-8
+    G = vecs.real.T @ vecs.real
+    assert np.abs(G - np.eye(10)).max() < 1e-10
+
+
+def test_eigenvectors_reference_order(pkg, orc):
+    m, n = 6, 6
+    lists = chain_lists(m)
+    h = pkg.Hamiltonian(pkg.Basis(m, n), lists)
+    ev, _, vec, _ = h.eigsh(0.2, 1.0, 0.1, nev=4, vectors=True)
+    _, _, _, rp, ci, tv, vd = oracle_H(orc, m, n, lists)
+    H = orc.full_csr(rp, ci, tv, vd, n, 0.2, 1.0, 0.1)
+    R = H @ vec - vec * ev
+    assert np.linalg.norm(R, axis=0).max() < 1e-9
+
+
+def test_mixed_precision_vs_fp64(pkg, golden):
+    rec = golden["irlm"]["m10n8"]
+    h = pkg.Hamiltonian(pkg.Basis(10, 8), chain_lists(10))
+    Js = np.array([0.05, 0.15, 0.25])
+    ev64, _, _, _ = h.eigsh_batch(Js, 1.0, 0.0, nev=10)
+    ev32, rs32, nc, info = h.eigsh_batch(Js, 1.0, 0.0, nev=10, precision=pkg.PREC_MIXED)
+    assert _rel(ev32, ev64) < RTOL_MIXED
+    assert _rel(ev64[1], rec["evals_sorted"]) < RTOL_FP64
+
+
+def test_tiny_dimensions(pkg, orc):
+    # D = 1 (n = 0), D = n + 1 (m = 2), D <= nev + block
+    for m, n, nev in [(3, 0, 1), (2, 3, 2), (3, 2, 4)]:
+        lists = chain_lists(m)
+        h = pkg.Hamiltonian(pkg.Basis(m, n), lists)
+        if h.D < 3 and nev > h.D:
+            continue
+        _, _, _, rp, ci, tv, vd = oracle_H(orc, m, n, lists)
+        H = orc.full_csr(rp, ci, tv, vd, n, 0.3, 1.0, 0.2).toarray()
+        w = np.linalg.eigvalsh(H)[:nev]
+        ev, _, _, _ = h.eigsh(0.3, 1.0, 0.2, nev=nev)
+        np.testing.assert_allclose(ev, w, rtol=1e-10, atol=1e-12)
+
+
+def test_nonconvergence_is_reported(pkg):
+    h = pkg.Hamiltonian(pkg.Basis(8, 8), chain_lists(8))
+    with pytest.raises(pkg.BHError, match="Eigenvalue computation failed"):
+        h.eigsh(0.1, 1.0, 0.5, nev=10, max_restarts=1, ncv=22)
