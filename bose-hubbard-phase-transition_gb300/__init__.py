@@ -46,7 +46,7 @@ class bh_solver_opts(C.Structure):
 class bh_solve_info(C.Structure):
     _fields_ = [
         ("nconv", C.c_int), ("restarts", C.c_int), ("matvecs", C.c_int64),
-        ("max_resid", C.c_double), ("seconds", C.c_double),
+        ("max_resid", C.c_double), ("seconds", C.c_double), ("launches", C.c_int64),
     ]
 
 
@@ -56,7 +56,8 @@ EXPORTS = [
     "bh_basis_info", "bh_basis_copy", "bh_basis_index", "bh_hamiltonian_create",
     "bh_hamiltonian_destroy", "bh_hamiltonian_nnz", "bh_hamiltonian_csr",
     "bh_hamiltonian_apply", "bh_solver_opts_default", "bh_eigsh", "bh_eigsh_csr",
-    "bh_eigsh_batch", "bh_gap_ratios", "bh_spdm", "bh_phase_map",
+    "bh_eigsh_batch", "bh_gap_ratios", "bh_spdm", "bh_phase_map", "bh_profile_enable",
+    "bh_profile_reset", "bh_profile_count", "bh_profile_get",
 ]
 
 _lib = None
@@ -100,6 +101,9 @@ def load() -> C.CDLL:
     L.bh_gap_ratios.argtypes = [C.c_int, vp, vp, f64p]
     L.bh_spdm.argtypes = [vp, C.c_int, vp, vp]
     L.bh_phase_map.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, vp, C.c_int, vp, vp, vp]
+    L.bh_profile_enable.argtypes = [C.c_int]
+    L.bh_profile_count.argtypes = [C.POINTER(C.c_int)]
+    L.bh_profile_get.argtypes = [C.c_int, C.c_char_p, C.c_int, i64p, f64p, f64p]
     _lib = L
     return L
 
@@ -213,6 +217,7 @@ class SolveInfo:
     matvecs: int
     max_resid: float
     seconds: float
+    launches: int
 
 
 class Hamiltonian:
@@ -289,7 +294,32 @@ class Hamiltonian:
 
 
 def _info(i: bh_solve_info) -> SolveInfo:
-    return SolveInfo(i.nconv, i.restarts, i.matvecs, i.max_resid, i.seconds)
+    return SolveInfo(i.nconv, i.restarts, i.matvecs, i.max_resid, i.seconds, i.launches)
+
+
+# ---------------------------------------------------------------------------
+# tracing: per-kernel device time (CUDA events) and algorithmic bytes
+# ---------------------------------------------------------------------------
+def profile_enable(on: bool = True):
+    _check(load().bh_profile_enable(int(bool(on))))
+
+
+def profile_reset():
+    _check(load().bh_profile_reset())
+
+
+def profile_read() -> dict:
+    """{kernel: {"launches", "ms", "bytes"}} accumulated since the last reset."""
+    L = load()
+    n = C.c_int()
+    _check(L.bh_profile_count(C.byref(n)))
+    out = {}
+    for i in range(n.value):
+        name = C.create_string_buffer(64)
+        k, ms, by = C.c_int64(), C.c_double(), C.c_double()
+        _check(L.bh_profile_get(i, name, 64, C.byref(k), C.byref(ms), C.byref(by)))
+        out[name.value.decode()] = {"launches": k.value, "ms": ms.value, "bytes": by.value}
+    return out
 
 
 # ---------------------------------------------------------------------------

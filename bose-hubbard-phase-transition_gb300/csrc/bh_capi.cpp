@@ -58,7 +58,7 @@ static SolveRequest make_request(const bh_solver_opts* o, int64_t D, int S) {
     if ((int64_t)p * 2 > D) p = 1;
     rq.p = p;
     BH_REQUIRE(o->nev <= D - 2 || (D <= 2 && o->nev <= D), "nb_eigen must be <= dimension - 2");
-    int kmax = o->ncv > 0 ? o->ncv : std::max(3 * o->nev, o->nev + 6 * p);
+    int kmax = o->ncv > 0 ? o->ncv : std::max(6 * o->nev, o->nev + 8 * p);
     kmax = (kmax + p - 1) / p * p;
     if (kmax > D) kmax = (int)(D / p * p);
     if (kmax < o->nev + p) {
@@ -86,6 +86,7 @@ static void fill_info(bh_solve_info* info, const SolveResult& r, int nev, double
     for (double v : r.resid) mx = std::max(mx, v);
     info->max_resid = mx;
     info->seconds = secs;
+    info->launches = r.launches;
 }
 
 }  // namespace bh
@@ -276,6 +277,7 @@ static OpView<double> op64_of(const bh_hamiltonian* h) {
     o.tv = h->d_tv64.p;
     o.vd = h->d_vd64.p;
     o.D = h->D;
+    o.rp_nnz = h->nnz;
     return o;
 }
 static OpView<float> op32_of(const bh_hamiltonian* h) {
@@ -285,6 +287,7 @@ static OpView<float> op32_of(const bh_hamiltonian* h) {
     o.tv = h->d_tv32.p;
     o.vd = h->d_vd32.p;
     o.D = h->D;
+    o.rp_nnz = h->nnz;
     return o;
 }
 
@@ -416,11 +419,13 @@ int bh_eigsh_csr(int64_t dim, const int64_t* row_ptr, const int32_t* col, const 
         a64.ci = ci.p;
         a64.tv = v64.p;
         a64.D = dim;
+        a64.rp_nnz = nnz;
         OpView<float> a32;
         a32.rp = rp.p;
         a32.ci = ci.p;
         a32.tv = v32.p;
         a32.D = dim;
+        a32.rp_nnz = nnz;
         SolveRequest rq = make_request(o, dim, 1);
         rq.want_vectors = evecs != nullptr;
         rq.J = {1.0};

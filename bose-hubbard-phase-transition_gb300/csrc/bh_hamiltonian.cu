@@ -69,7 +69,8 @@ k_csr_rows(uint32_t D, int m, int n, const uint32_t* __restrict__ rt,
                     a += 0.5 * x * (x - 1.0);
                 }
                 col[s] = (int)row;
-                v[s] = U * a + shift;
+                // (U V) + (-mu n) with one rounding each, no contraction
+                v[s] = __dadd_rn(__dmul_rn(U, a), shift);
                 ok[s] = true;
             }
         }

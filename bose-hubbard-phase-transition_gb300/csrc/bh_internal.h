@@ -157,6 +157,12 @@ Lists square_lists(int m, bool closed);
 Lists cube_lists(int m, bool closed);
 void flatten(const Lists& nb, int32_t* off, int32_t* out, int cap, int* count);
 
+// ---- optional per-kernel timing (bh_profile.cpp) ----
+bool profile_on();
+void profile_begin(cudaStream_t st);
+void profile_end(cudaStream_t st, const char* name, double bytes);
+void profile_flush();
+
 // ---- host dense symmetric eigensolver (bh_symeig.cpp) ----
 // a: n x n column-major symmetric, overwritten with eigenvectors (columns);
 // w: eigenvalues ascending.  Returns false if the iteration did not converge.

@@ -8,22 +8,30 @@
 // of a phase-diagram grid: H = J T + U V - mu N) run in lock-step as one
 // batch.  Every Krylov block of the batch is one row-major D x (S p) array, so
 // one SpMM streams T once per step for all S p vectors and every gathered row
-// of X is a contiguous S p-vector.  Per step (block Lanczos with full
-// re-orthogonalisation by classical Gram-Schmidt applied twice):
-//     W = H V_j                                   k_spmm
-//     C = [V_0..V_j]^T W,  W -= [V_0..V_j] C      k_dot + k_dot_finalize + k_update  (x2)
-//     W = V_{j+1} R  (Cholesky QR of W^T W)       k_update(gram) + k_qr_finalize + k_normalize
-// The projected matrix T (FP64) is filled on the device from C and R; the
-// host reads it only at a restart, solves the small eigenproblems in FP64,
-// and sends back the Ritz rotation applied by k_rotate (thick restart).
-// Vectors are FP64 (plain method) or FP32 (mixed); the coefficients C, R and
-// all reductions are FP64 (FP32 partial sums over at most 32 rows are folded
-// into FP64 accumulators).  A final FP64 Rayleigh-Ritz on the Ritz vectors
-// (FP64 SpMM, FP64 Gram matrices, FP64 generalised eigensolve) gives the
-// returned eigenvalues and their true FP64 residuals.
+// of X is a contiguous S p-vector.  Per block step j:
+//     W  = H V_j                                         k_spmm
+//     A  = V_j^T W;  W -= V_j A + V_{j-1} R_{j-1}^T      k_dot + k_local_coef + k_update
+//          (after a thick restart: + V_keep S^T, the arrowhead coupling)
+//     C  = [V_0..V_j]^T W;  W -= [V_0..V_j] C            k_dot + k_dot_finalize + k_update
+//          (one full classical Gram-Schmidt re-orthogonalisation pass; the
+//           Gram matrix W^T W is accumulated in the same pass)
+//     W  = V_{j+1} R  (Cholesky QR)                      k_qr_finalize + k_normalize
+// The projected matrix T (FP64) is assembled on the device from A, R and C;
+// the host reads it only at a restart, solves the small eigenproblems in FP64,
+// and sends back the Ritz rotation applied by k_rotate.  At each restart the
+// solves that have converged are retired (their Ritz vectors are rotated out)
+// and the remaining ones are compacted into a narrower batch.
+//
+// Vectors are FP64 (plain method) or FP32 (mixed); the coefficients A, C, R
+// and all reductions are FP64 (FP32 partial sums over at most 32 rows are
+// folded into FP64 accumulators).  A final FP64 Rayleigh-Ritz on the Ritz
+// vectors (FP64 SpMM, FP64 Gram matrices, FP64 generalised eigensolve) gives
+// the returned eigenvalues and their true FP64 residuals.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <numeric>
 #include <thread>
 #include <type_traits>
 
@@ -159,12 +167,45 @@ __global__ void k_dot_finalize(int nchunks, int kc, int ncols, int ldC, int p, i
     }
 }
 
+// Coefficients of the local block-Lanczos step for column block j, rows
+// c in [c_lo, (j+1) p):
+//   rows of block j      : A = V_j^T W (from the chunk partials of a 1-block k_dot)
+//   rows below block j   : the known couplings of the new block with the
+//                          earlier columns, T_s[j p + q'][c] (lower part:
+//                          R_{j-1} from the previous QR, or the arrowhead rows
+//                          written at a thick restart)
+// Cf[(c - c_lo)][s p + q'] receives them, and T_s[c][j p + q'] += them.
+template <class T>
+__global__ void k_local_coef(int nchunks, int j, int c_lo, int ncols, int p, int kcap,
+                             const double* __restrict__ part, double* __restrict__ Tm, int Tdim,
+                             T* __restrict__ Cf) {
+    const int rows = (j + 1) * p - c_lo;
+    const int total = rows * ncols;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+        const int cr = idx / ncols, t = idx % ncols;
+        const int c = c_lo + cr;
+        const int s = t / p, q = t % p;
+        double* Ts = Tm + (size_t)s * Tdim * Tdim;
+        double v;
+        if (c >= j * p) {
+            v = 0.0;
+            for (int ch = 0; ch < nchunks; ++ch) v += part[((size_t)ch * kcap + (c - j * p)) * ncols + t];
+        } else {
+            v = Ts[(size_t)c * Tdim + j * p + q];
+        }
+        Cf[(size_t)cr * ncols + t] = (T)v;
+        Ts[(size_t)(j * p + q) * Tdim + c] += v;
+    }
+}
+
 // W[r][s p + q'] -= sum_{c < kc} V_{c/p}[r][s p + c%p] Cf[c][s p + q'], then
 // (optionally) Gram partials G_s[q][q'] = sum_r W[r][s p + q] W[r][s p + q'].
+// Two rows per iteration and four columns of C per inner step keep eight
+// independent loads in flight per thread.
 template <class T, int PMAX>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(256)
 k_update(int64_t D, int ncols, int p, int lp, int kc, int64_t bstride, const T* __restrict__ V,
-         const T* __restrict__ Cf, T* __restrict__ W, int64_t rows_per_chunk, int do_gram,
+         const T* __restrict__ Cf, T* __restrict__ W, int64_t rows_per_cta, int do_gram,
          double* __restrict__ gpart) {
     extern __shared__ __align__(16) unsigned char s_raw[];
     T* sC = reinterpret_cast<T*>(s_raw);
@@ -172,10 +213,10 @@ k_update(int64_t D, int ncols, int p, int lp, int kc, int64_t bstride, const T* 
     for (int i = threadIdx.x; i < kc * ncols; i += blockDim.x) sC[i] = Cf[i];
     __syncthreads();
     const int t = threadIdx.x % ncols, ro = threadIdx.x / ncols, R = blockDim.x / ncols;
-    const int s = t / p, q = t % p;
+    const int s = t / p, q = t % p, pm = p - 1;
     const int lane = threadIdx.x & 31;
-    const int64_t r0 = (int64_t)blockIdx.x * rows_per_chunk;
-    const int64_t r1 = min(D, r0 + rows_per_chunk);
+    const int64_t r0 = (int64_t)blockIdx.x * rows_per_cta;
+    const int64_t r1 = min(D, r0 + rows_per_cta);
     double gd[PMAX];
     T gf[PMAX];
 #pragma unroll
@@ -184,33 +225,57 @@ k_update(int64_t D, int ncols, int p, int lp, int kc, int64_t bstride, const T* 
         gf[b] = T(0);
     }
     int cnt = 0;
-    for (int64_t base = r0; base < r1; base += R) {
-        const int64_t r = base + ro;
-        const bool valid = r < r1;
-        T w = valid ? W[r * ncols + t] : T(0);
-        if (valid && kc > 0) {
-            const T* vr = V + r * ncols + s * p;
+    for (int64_t base = r0; base < r1; base += 2 * R) {
+        const int64_t rA = base + ro, rB = rA + R;
+        const bool vA = rA < r1, vB = rB < r1;
+        T wA = vA ? W[rA * ncols + t] : T(0);
+        T wB = vB ? W[rB * ncols + t] : T(0);
+        if (kc > 0 && (vA || vB)) {
+            const T* pA = V + (vA ? rA : r0) * ncols + s * p;
+            const T* pB = V + (vB ? rB : r0) * ncols + s * p;
             T a0 = T(0), a1 = T(0), a2 = T(0), a3 = T(0);
+            T b0 = T(0), b1 = T(0), b2 = T(0), b3 = T(0);
             int c = 0;
             for (; c + 3 < kc; c += 4) {
-                a0 += vr[(int64_t)(c >> lp) * bstride + (c & (p - 1))] * sC[c * ncols + t];
-                a1 += vr[(int64_t)((c + 1) >> lp) * bstride + ((c + 1) & (p - 1))] * sC[(c + 1) * ncols + t];
-                a2 += vr[(int64_t)((c + 2) >> lp) * bstride + ((c + 2) & (p - 1))] * sC[(c + 2) * ncols + t];
-                a3 += vr[(int64_t)((c + 3) >> lp) * bstride + ((c + 3) & (p - 1))] * sC[(c + 3) * ncols + t];
+                const int64_t o0 = (int64_t)(c >> lp) * bstride + (c & pm);
+                const int64_t o1 = (int64_t)((c + 1) >> lp) * bstride + ((c + 1) & pm);
+                const int64_t o2 = (int64_t)((c + 2) >> lp) * bstride + ((c + 2) & pm);
+                const int64_t o3 = (int64_t)((c + 3) >> lp) * bstride + ((c + 3) & pm);
+                const T x0 = pA[o0], x1 = pA[o1], x2 = pA[o2], x3 = pA[o3];
+                const T y0 = pB[o0], y1 = pB[o1], y2 = pB[o2], y3 = pB[o3];
+                const T k0 = sC[c * ncols + t], k1 = sC[(c + 1) * ncols + t];
+                const T k2 = sC[(c + 2) * ncols + t], k3 = sC[(c + 3) * ncols + t];
+                a0 += x0 * k0;
+                a1 += x1 * k1;
+                a2 += x2 * k2;
+                a3 += x3 * k3;
+                b0 += y0 * k0;
+                b1 += y1 * k1;
+                b2 += y2 * k2;
+                b3 += y3 * k3;
             }
-            for (; c < kc; ++c) a0 += vr[(int64_t)(c >> lp) * bstride + (c & (p - 1))] * sC[c * ncols + t];
-            w -= (a0 + a1) + (a2 + a3);
-            W[r * ncols + t] = w;
+            for (; c < kc; ++c) {
+                const int64_t o0 = (int64_t)(c >> lp) * bstride + (c & pm);
+                const T k0 = sC[c * ncols + t];
+                a0 += pA[o0] * k0;
+                b0 += pB[o0] * k0;
+            }
+            // rows past the chunk end read a valid row but must stay zero
+            wA = vA ? wA - ((a0 + a1) + (a2 + a3)) : T(0);
+            wB = vB ? wB - ((b0 + b1) + (b2 + b3)) : T(0);
+            if (vA) W[rA * ncols + t] = wA;
+            if (vB) W[rB * ncols + t] = wB;
         }
         if (do_gram) {
 #pragma unroll
             for (int b = 0; b < PMAX; ++b) {
                 if (b < p) {
-                    const T wb = __shfl_sync(0xffffffffu, w, lane - q + b);
-                    gf[b] += wb * w;
+                    const T xa = __shfl_sync(0xffffffffu, wA, lane - q + b);
+                    const T xb = __shfl_sync(0xffffffffu, wB, lane - q + b);
+                    gf[b] += xa * wA + xb * wB;
                 }
             }
-            if (++cnt == 32) {
+            if (++cnt == 16) {
                 cnt = 0;
 #pragma unroll
                 for (int b = 0; b < PMAX; ++b) {
@@ -233,37 +298,63 @@ k_update(int64_t D, int ncols, int p, int lp, int kc, int64_t bstride, const T* 
     }
 }
 
-// One thread per solve: G = sum of Gram partials, Cholesky G = R^T R (R upper
-// triangular), Rinv = R^{-1}; T_s[(jrow p + a)][(jrow - 1) p + b] = R[a][b].
-// A pivot below tiny^2 (relative to the solve's scale) is a breakdown: the
-// direction is dropped (zero column of Rinv) and brk[s] records jrow.
-__global__ void k_qr_finalize(int S, int p, int nchunks, int ncols, const double* __restrict__ gpart,
-                              double* __restrict__ Rinv, double* __restrict__ Tm, int Tdim,
-                              int jrow, const double* __restrict__ scale, double rel_tiny,
-                              int* __restrict__ brk) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= S) return;
-    double G[16][16], R[16][16], Ri[16][16];
+// One CTA per solve: G = sum of the Gram partials (fixed-order tree
+// reduction), then one pass of the block orthonormalisation W = Q R:
+//   mode 0  shifted Cholesky  G + s I = R^T R, s = shift_rel * max_i G_ii,
+//           which always exists and bounds cond(W R^{-1}); Racc <- R
+//   mode 1  Cholesky G = R^T R;  Racc <- R Racc
+//   mode 2  Cholesky G = R^T R;  Rtot = R Racc is the block coupling,
+//           written to T_s[(jrow p + a)][(jrow - 1) p + b]  (final pass)
+// (shifted CholQR3: the product of the three factors is exact, and the
+// last two passes restore orthonormality to working precision).  For p = 1
+// a single mode-2 pass normalises the vector.  In the final pass a
+// direction whose norm |Rtot_ii| is below kill_abs * (its norm before
+// orthogonalisation) is numerically inside the span of the basis: it is
+// dropped (zero column of Rinv, zero row of the coupling, dead flag set).
+// The norm before orthogonalisation is sqrt(sum_c T[c][col]^2 + |Rtot_.i|^2)
+// with col = (jrow - 1) p + i, the coefficients of H v_col in the basis.
+constexpr int QR_THREADS = 128;
+__global__ void __launch_bounds__(QR_THREADS)
+k_qr_finalize(int p, int nchunks, int ncols, const double* __restrict__ gpart, int mode,
+              double shift_rel, double* __restrict__ Racc, double* __restrict__ Rinv,
+              double* __restrict__ Tm, int Tdim, int jrow, double kill_abs,
+              unsigned char* __restrict__ dead) {
+    __shared__ double red[QR_THREADS];
+    __shared__ double G[16][16];
+    const int s = blockIdx.x;
+    for (int e = 0; e < p * p; ++e) {
+        const int a = e / p, b = e % p;
+        double v = 0.0;
+        for (int ch = threadIdx.x; ch < nchunks; ch += QR_THREADS)
+            v += gpart[((size_t)ch * p + a) * ncols + s * p + b];
+        red[threadIdx.x] = v;
+        __syncthreads();
+        for (int off = QR_THREADS / 2; off > 0; off >>= 1) {
+            if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) G[a][b] = red[0];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    double R[16][16], Ri[16][16], Rt[16][16];
     for (int a = 0; a < p; ++a)
         for (int b = 0; b < p; ++b) {
-            double sum = 0.0;
-            for (int ch = 0; ch < nchunks; ++ch) sum += gpart[((size_t)ch * p + a) * ncols + s * p + b];
-            G[a][b] = sum;
             R[a][b] = 0.0;
             Ri[a][b] = 0.0;
+            Rt[a][b] = 0.0;
         }
-    const double sc = scale ? scale[s] : 1.0;
-    const double tiny = rel_tiny * (sc > 0.0 ? sc : 1.0);
-    bool broke = false;
+    double shift = 0.0;
+    if (mode == 0) {
+        double gmax = 0.0;
+        for (int i = 0; i < p; ++i) gmax = fmax(gmax, G[i][i]);
+        shift = shift_rel * gmax;
+    }
+    double* Ra = Racc + (size_t)s * p * p;
     for (int i = 0; i < p; ++i) {
-        double d = 0.5 * (G[i][i] + G[i][i]);
+        double d = G[i][i] + shift;
         for (int k = 0; k < i; ++k) d -= R[k][i] * R[k][i];
-        if (!(d > tiny * tiny)) {
-            broke = true;
-            R[i][i] = 0.0;
-            for (int j = i + 1; j < p; ++j) R[i][j] = 0.0;
-            continue;
-        }
+        if (!(d > 0.0)) continue;  // zero column (already dropped) stays zero
         const double rii = sqrt(d);
         R[i][i] = rii;
         for (int j = i + 1; j < p; ++j) {
@@ -272,8 +363,33 @@ __global__ void k_qr_finalize(int S, int p, int nchunks, int ncols, const double
             R[i][j] = v / rii;
         }
     }
-    // inverse of the upper-triangular R (dropped directions stay zero)
+    // accumulated factor Rt = R * Racc (upper triangular products)
+    for (int a = 0; a < p; ++a)
+        for (int b = 0; b < p; ++b) {
+            if (mode == 0 || p == 1) {
+                Rt[a][b] = R[a][b];
+            } else {
+                double v = 0.0;
+                for (int k = a; k <= b; ++k) v += R[a][k] * Ra[k * p + b];
+                Rt[a][b] = v;
+            }
+        }
+    const bool final_pass = mode == 2;
+    bool drop[16];
+    for (int i = 0; i < p; ++i) drop[i] = R[i][i] == 0.0;
+    if (final_pass && Tm && jrow > 0) {
+        const double* Ts = Tm + (size_t)s * Tdim * Tdim;
+        for (int i = 0; i < p; ++i) {
+            double pre = 0.0, own = 0.0;
+            const int col = (jrow - 1) * p + i;
+            for (int c = 0; c < jrow * p; ++c) pre += Ts[(size_t)col * Tdim + c] * Ts[(size_t)col * Tdim + c];
+            for (int k = 0; k <= i; ++k) own += Rt[k][i] * Rt[k][i];
+            if (!(fabs(Rt[i][i]) > kill_abs * sqrt(pre + own))) drop[i] = true;
+        }
+    }
+    // inverse of this pass's R on the kept directions
     for (int j = 0; j < p; ++j) {
+        if (drop[j] && final_pass) continue;
         if (R[j][j] == 0.0) continue;
         Ri[j][j] = 1.0 / R[j][j];
         for (int i = j - 1; i >= 0; --i) {
@@ -285,12 +401,17 @@ __global__ void k_qr_finalize(int S, int p, int nchunks, int ncols, const double
     }
     for (int a = 0; a < p; ++a)
         for (int b = 0; b < p; ++b) Rinv[(size_t)s * p * p + a * p + b] = Ri[a][b];
+    for (int a = 0; a < p; ++a)
+        for (int b = 0; b < p; ++b) Ra[a * p + b] = (final_pass && drop[a]) ? 0.0 : Rt[a][b];
+    if (!final_pass) return;
     if (Tm && jrow > 0) {
-        double* Ts = Tm + (size_t)s * Tdim * Tdim;
+        double* Tw = Tm + (size_t)s * Tdim * Tdim;
         for (int a = 0; a < p; ++a)
-            for (int b = 0; b < p; ++b) Ts[(size_t)((jrow - 1) * p + b) * Tdim + jrow * p + a] = R[a][b];
+            for (int b = 0; b < p; ++b)
+                Tw[(size_t)((jrow - 1) * p + b) * Tdim + jrow * p + a] = drop[a] ? 0.0 : Rt[a][b];
+        if (dead)
+            for (int a = 0; a < p; ++a) dead[(size_t)s * Tdim + jrow * p + a] = drop[a] ? 1 : 0;
     }
-    if (broke && brk && brk[s] < 0) brk[s] = jrow;
 }
 
 // V[r][s p + q'] = sum_{q <= q'} W[r][s p + q] Rinv_s[q][q']
@@ -311,56 +432,76 @@ __global__ void k_normalize(int64_t D, int ncols, int p, const double* __restric
     }
 }
 
-// Thick-restart rotation: out_s[:, i] = sum_{c < kc} V_s[:, c] Y_s[c][i], i < nout.
-// Input column c of solve s is V_{c/p}[r][s p + c%p].  Output layout: blocks of
-// p columns (Vout[i/p][r][s p + i%p], stride ostride) or, when out_cols > 0, one
-// row-major block Vout[r][s nout + i] with out_cols = S nout columns.
+// Ritz rotation: for the processed solves ls < Sproc (input solve in_idx[ls],
+// output slot out_idx[ls]):  out[:, i] = sum_{c < kc} V[:, c] Y_ls[c][i].
+// Input column c of solve s is V_{c/p}[r][s p + c%p] (row stride ld_in).
+// Output: blocks of p columns  Vout[i/p][r][o p + i%p]  (block stride
+// ostride, row stride ld_out), or with single != 0 one row-major array
+// Vout[r][o nout + i].  Each thread owns one (solve, column-in-block) lane
+// of one row and produces its outputs eight at a time.
 template <class T>
 __global__ void __launch_bounds__(256)
-k_rotate(int64_t D, int S, int ncols, int p, int kc, int nout, int64_t bstride,
-         const T* __restrict__ V, const T* __restrict__ Yg, T* __restrict__ Vout, int64_t ostride,
-         int out_cols, int Sg, int64_t rows_per_chunk) {
+k_rotate(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t bstride,
+         const T* __restrict__ V, const T* __restrict__ Yg, const int* __restrict__ in_idx,
+         const int* __restrict__ out_idx, T* __restrict__ Vout, int64_t ostride, int ld_out,
+         int single, int Sg, int ystride, int64_t rows_per_chunk) {
     extern __shared__ __align__(16) unsigned char s_raw[];
     T* sY = reinterpret_cast<T*>(s_raw);
     const int sg0 = blockIdx.y * Sg;
-    const int nsg = min(Sg, S - sg0);
-    for (int i = threadIdx.x; i < nsg * kc * nout; i += blockDim.x) sY[i] = Yg[(size_t)sg0 * kc * nout + i];
+    const int nsg = min(Sg, Sproc - sg0);
+    for (int i = threadIdx.x; i < nsg * kc * nout; i += blockDim.x) {
+        const int ls = i / (kc * nout), e = i - ls * (kc * nout);
+        sY[(size_t)ls * ystride + e] = Yg[(size_t)(sg0 + ls) * kc * nout + e];
+    }
     __syncthreads();
     const int width = Sg * p;
     const int tl = threadIdx.x % width, ro = threadIdx.x / width, R = blockDim.x / width;
     const int ls = tl / p, qo = tl % p;
     if (ls >= nsg) return;
-    const int s = sg0 + ls;
+    const int sin = in_idx[sg0 + ls], sout = out_idx[sg0 + ls];
     const int nob = nout / p;
     const int64_t r0 = (int64_t)blockIdx.x * rows_per_chunk;
     const int64_t r1 = min(D, r0 + rows_per_chunk);
-    const T* ys = sY + (size_t)ls * kc * nout;
+    const T* ys = sY + (size_t)ls * ystride;
     for (int64_t r = r0 + ro; r < r1; r += R) {
+        const T* vr = V + r * ld_in + sin * p;
         for (int jo0 = 0; jo0 < nob; jo0 += 8) {
             T acc[8];
 #pragma unroll
             for (int u = 0; u < 8; ++u) acc[u] = T(0);
-            for (int j = 0; j < kc / p; ++j) {
-                const T* vr = V + (int64_t)j * bstride + r * ncols + s * p;
-                for (int q = 0; q < p; ++q) {
-                    const T v = vr[q];
-                    const T* yrow = ys + (size_t)(j * p + q) * nout + qo;
+            for (int c = 0; c < kc; ++c) {
+                const T x = vr[(int64_t)(c / p) * bstride + c % p];
+                const T* yr = ys + (size_t)c * nout + qo + jo0 * p;
 #pragma unroll
-                    for (int u = 0; u < 8; ++u)
-                        if (jo0 + u < nob) acc[u] += v * yrow[(jo0 + u) * p];
-                }
+                for (int u = 0; u < 8; ++u)
+                    if (jo0 + u < nob) acc[u] += x * yr[u * p];
             }
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
                 if (jo0 + u < nob) {
                     const int i = (jo0 + u) * p + qo;
-                    if (out_cols > 0)
-                        Vout[r * out_cols + (int64_t)s * nout + i] = acc[u];
+                    if (single)
+                        Vout[r * ld_out + (int64_t)sout * nout + i] = acc[u];
                     else
-                        Vout[(int64_t)(jo0 + u) * ostride + r * ncols + s * p + qo] = acc[u];
+                        Vout[(int64_t)(jo0 + u) * ostride + r * ld_out + sout * p + qo] = acc[u];
                 }
             }
         }
+    }
+}
+
+// Vout[r][a p + q] = Vin[r][in_idx[a] p + q]  (compaction of one block)
+template <class T>
+__global__ void k_gather_block(int64_t D, int Snew, int p, int ld_in, int ld_out,
+                               const int* __restrict__ in_idx, const T* __restrict__ Vin,
+                               T* __restrict__ Vout) {
+    const int64_t total = D * ld_out;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = idx / ld_out;
+        const int t = (int)(idx - r * ld_out);
+        const int a = t / p, q = t % p;
+        Vout[idx] = Vin[r * ld_in + in_idx[a] * p + q];
     }
 }
 
@@ -473,6 +614,17 @@ static bool verbose() {
     return v == 1;
 }
 
+// BH_DEBUG_ORTHO=1 additionally measures the orthogonality of the Krylov basis
+// of the first active solve at every restart (diagnostic; costs one Gram pass).
+static bool debug_ortho() {
+    static int v = -1;
+    if (v < 0) {
+        const char* e = std::getenv("BH_DEBUG_ORTHO");
+        v = (e && *e && *e != '0') ? 1 : 0;
+    }
+    return v == 1;
+}
+
 static int ilog2(int p) {
     int l = 0;
     while ((1 << l) < p) ++l;
@@ -495,7 +647,7 @@ static void parallel_for(int n, F&& f) {
     for (auto& t : th) t.join();
 }
 
-// geometry of the row-chunked reductions
+// geometry of the row-chunked reductions (k_dot, k_resid): at most 2 chunks per SM
 struct Geo {
     int ncols = 0, R = 1, NT = 0;
     int64_t rows_per_chunk = 0;
@@ -516,6 +668,22 @@ static Geo make_geo(int64_t D, int ncols) {
     return g;
 }
 
+// geometry of k_update: many small CTAs (each handles >= 16 R rows)
+static Geo make_ugeo(int64_t D, int ncols) {
+    Geo g;
+    g.ncols = ncols;
+    g.R = std::max(1, 256 / ncols);
+    g.NT = ncols * g.R;
+    const int64_t target = 16LL * sm_count();
+    int64_t rpc = (D + target - 1) / target;
+    rpc = std::max<int64_t>(rpc, (int64_t)g.R * 16);
+    rpc = (rpc + 2 * g.R - 1) / (2 * g.R) * (2 * g.R);
+    g.rows_per_chunk = rpc;
+    g.nchunks = (int)((D + rpc - 1) / rpc);
+    if (g.nchunks < 1) g.nchunks = 1;
+    return g;
+}
+
 static unsigned elem_grid(int64_t n, int threads = 256) {
     int64_t g = (n + threads - 1) / threads;
     const int64_t cap = (int64_t)sm_count() * 8;
@@ -528,6 +696,12 @@ struct Launcher {
     cudaStream_t st;
     int64_t* launches;
 
+    void done(const char* name, double bytes) const {
+        BH_CUDA(cudaGetLastError());
+        ++*launches;
+        profile_end(st, name, bytes);
+    }
+
     void spmm(int ncols, int group, const double* prm, const T* X, T* Y) const {
         const int64_t D = op.D;
         int L = 1;
@@ -536,6 +710,7 @@ struct Launcher {
         int64_t g = (D + rpb - 1) / rpb;
         g = std::min<int64_t>(g, (int64_t)sm_count() * 16);
         g = std::max<int64_t>(g, 1);
+        profile_begin(st);
         switch (L) {
             case 1: k_spmm<T, 1><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y); break;
             case 2: k_spmm<T, 2><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y); break;
@@ -544,8 +719,9 @@ struct Launcher {
             case 16: k_spmm<T, 16><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y); break;
             default: k_spmm<T, 32><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y); break;
         }
-        BH_CUDA(cudaGetLastError());
-        ++*launches;
+        const double nnz = (double)op.rp_nnz;
+        done("k_spmm", nnz * (4.0 + sizeof(T)) + (double)(D + 1) * 8.0 + (op.vd ? (double)D * sizeof(T) : 0.0) +
+                           2.0 * (double)D * ncols * sizeof(T));
     }
 
     template <int PMAX>
@@ -556,9 +732,9 @@ struct Launcher {
         const size_t smem = (size_t)g.NT * JT * PMAX * sizeof(double);
         auto kern = k_dot<T, PMAX, JT>;
         if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        profile_begin(st);
         kern<<<grid, g.NT, smem, st>>>(op.D, g.ncols, ld, p, nblk, bstride, V, W, g.rows_per_chunk, kcap, part);
-        BH_CUDA(cudaGetLastError());
-        ++*launches;
+        done("k_dot", (double)(nblk + 1) * op.D * g.ncols * sizeof(T));
     }
     void dot(const Geo& g, int ld, int p, int nblk, int64_t bstride, const T* V, const T* W,
              int kcap, double* part) const {
@@ -571,10 +747,18 @@ struct Launcher {
     }
     void dot_finalize(const Geo& g, int kc, int ldC, int p, int kcap, const double* part, double* C,
                       T* Cf, double* Tm, int Tdim, int jcol) const {
+        profile_begin(st);
         k_dot_finalize<T><<<elem_grid((int64_t)kc * g.ncols), 256, 0, st>>>(
             g.nchunks, kc, g.ncols, ldC, p, kcap, part, C, Cf, Tm, Tdim, jcol);
-        BH_CUDA(cudaGetLastError());
-        ++*launches;
+        done("k_dot_finalize", (double)g.nchunks * kc * g.ncols * 8.0);
+    }
+    void local_coef(const Geo& g, int j, int c_lo, int p, int kcap, const double* part, double* Tm,
+                    int Tdim, T* Cf) const {
+        const int64_t total = (int64_t)((j + 1) * p - c_lo) * g.ncols;
+        profile_begin(st);
+        k_local_coef<T><<<elem_grid(total), 256, 0, st>>>(g.nchunks, j, c_lo, g.ncols, p, kcap, part,
+                                                          Tm, Tdim, Cf);
+        done("k_local_coef", (double)g.nchunks * p * g.ncols * 8.0);
     }
     template <int PMAX>
     void update_t(const Geo& g, int p, int kc, int64_t bstride, const T* V, const T* Cf, T* W,
@@ -584,10 +768,11 @@ struct Launcher {
         if ((int)smem > max_smem_optin()) throw Error(BH_ERR_ARG, "Krylov basis too wide for shared memory (reduce ncv or batch)");
         auto kern = k_update<T, PMAX>;
         if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        profile_begin(st);
         kern<<<g.nchunks, g.NT, smem, st>>>(op.D, g.ncols, p, ilog2(p), kc, bstride, V, Cf, W,
                                             g.rows_per_chunk, do_gram, gpart);
-        BH_CUDA(cudaGetLastError());
-        ++*launches;
+        done(kc > 0 ? "k_update" : "k_update(gram)",
+             (double)(kc > 0 ? kc + 2 : 1) * op.D * g.ncols * sizeof(T));
     }
     void update(const Geo& g, int p, int kc, int64_t bstride, const T* V, const T* Cf, T* W,
                 int do_gram, double* gpart) const {
@@ -597,41 +782,56 @@ struct Launcher {
         else if (p <= 8) update_t<8>(g, p, kc, bstride, V, Cf, W, do_gram, gpart);
         else update_t<16>(g, p, kc, bstride, V, Cf, W, do_gram, gpart);
     }
-    void qr(const Geo& g, int S, int p, const double* gpart, double* Rinv, double* Tm, int Tdim,
-            int jrow, const double* scale, double rel_tiny, int* brk) const {
-        k_qr_finalize<<<(S + 63) / 64, 64, 0, st>>>(S, p, g.nchunks, g.ncols, gpart, Rinv, Tm, Tdim,
-                                                   jrow, scale, rel_tiny, brk);
-        BH_CUDA(cudaGetLastError());
-        ++*launches;
+    void qr(const Geo& gu, int S, int p, const double* gpart, int mode, double shift_rel,
+            double* Racc, double* Rinv, double* Tm, int Tdim, int jrow, double kill_abs,
+            unsigned char* dead) const {
+        profile_begin(st);
+        k_qr_finalize<<<S, QR_THREADS, 0, st>>>(p, gu.nchunks, gu.ncols, gpart, mode, shift_rel, Racc,
+                                                Rinv, Tm, Tdim, jrow, kill_abs, dead);
+        done("k_qr_finalize", (double)gu.nchunks * p * gu.ncols * 8.0);
     }
     void normalize(int ncols, int p, const double* Rinv, const T* W, T* Vout) const {
+        profile_begin(st);
         k_normalize<T><<<elem_grid(op.D * ncols), 256, 0, st>>>(op.D, ncols, p, Rinv, W, Vout);
-        BH_CUDA(cudaGetLastError());
-        ++*launches;
+        done("k_normalize", 2.0 * op.D * ncols * sizeof(T));
     }
-    void rotate(int S, int ncols, int p, int kc, int nout, int64_t bstride, const T* V,
-                const T* Yg, T* Vout, int64_t ostride, int out_cols) const {
-        const int smax = max_smem_optin();
-        const size_t per = (size_t)kc * nout * sizeof(T);
+    // rotation of Sproc solves (see k_rotate); Yg is Sproc x kc x nout
+    void rotate(int Sproc, int ld_in, int p, int kc, int nout, int64_t bstride, const T* V,
+                const T* Yg, const int* in_idx, const int* out_idx, T* Vout, int64_t ostride,
+                int ld_out, int single) const {
+        if (Sproc <= 0) return;
+        const int smax = std::min(max_smem_optin(), 160 * 1024);
+        const int ystride = (kc * nout) | 1;  // odd: solves land on different banks
+        const size_t per = (size_t)ystride * sizeof(T);
         if ((int)per > smax) throw Error(BH_ERR_ARG, "restart rotation too large for shared memory (reduce ncv)");
-        int Sg = (int)std::min<size_t>((size_t)S, std::max<size_t>(1, (size_t)(48 * 1024) / per));
-        Sg = std::min(Sg, std::max(1, 256 / p));
+        int Sg = (int)std::min<size_t>((size_t)Sproc, std::max<size_t>(1, (size_t)(64 * 1024) / per));
+        Sg = std::min(Sg, std::max(1, 128 / p));
         while (Sg > 1 && 256 % (Sg * p) != 0) --Sg;
         const size_t smem = (size_t)Sg * per;
         const int width = Sg * p;
-        const int NT = 256 / width * width;
-        const int64_t target = 2LL * sm_count();
-        const int ngroups = (S + Sg - 1) / Sg;
-        int64_t chunks = std::max<int64_t>(1, target / ngroups);
+        const int NT = std::max(width, 256 / width * width);
+        const int ngroups = (Sproc + Sg - 1) / Sg;
+        const int R = NT / width;
+        int64_t chunks = std::max<int64_t>(1, (4LL * sm_count()) / ngroups);
         int64_t rpc = (op.D + chunks - 1) / chunks;
-        rpc = std::max<int64_t>(rpc, 1);
+        rpc = std::max<int64_t>(rpc, 2LL * R);
         chunks = (op.D + rpc - 1) / rpc;
-        auto kern = k_rotate<T>;
-        if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        kern<<<dim3((unsigned)std::max<int64_t>(chunks, 1), ngroups), NT, smem, st>>>(
-            op.D, S, ncols, p, kc, nout, bstride, V, Yg, Vout, ostride, out_cols, Sg, rpc);
-        BH_CUDA(cudaGetLastError());
-        ++*launches;
+        auto launch = [&](auto kern) {
+            if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            kern<<<dim3((unsigned)chunks, ngroups), NT, smem, st>>>(
+                op.D, Sproc, ld_in, p, kc, nout, bstride, V, Yg, in_idx, out_idx, Vout, ostride,
+                ld_out, single, Sg, ystride, rpc);
+        };
+        profile_begin(st);
+        launch(k_rotate<T>);
+        done("k_rotate", (double)op.D * Sproc * p * ((double)kc / p + (double)nout / p) * sizeof(T));
+    }
+    void gather_block(int Snew, int p, int ld_in, int ld_out, const int* in_idx, const T* Vin,
+                      T* Vout) const {
+        profile_begin(st);
+        k_gather_block<T><<<elem_grid(op.D * ld_out), 256, 0, st>>>(op.D, Snew, p, ld_in, ld_out,
+                                                                     in_idx, Vin, Vout);
+        done("k_gather_block", 2.0 * op.D * ld_out * sizeof(T));
     }
 };
 
@@ -654,200 +854,345 @@ static bool cholesky_lower(int n, std::vector<double>& a) {  // a = L L^T, L in 
 }
 
 // ---------------------------------------------------------------------------
-// the solver
+// the Lanczos phase (precision T for vectors)
 // ---------------------------------------------------------------------------
 
 template <class T>
-static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq, const double* d_prm,
-                          const double* d_scale_init, cudaStream_t st, SolveResult& res,
+static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
+                          const std::vector<double>& prm_all, cudaStream_t st, SolveResult& res,
                           int K, DevBuf<T>& Xout, std::vector<double>& theta_out) {
     const int64_t D = op.D;
-    const int S = rq.S, p = rq.p, ncols = S * p;
+    const int S0 = rq.S, p = rq.p;
     const int kmax = rq.kmax, nb = kmax / p, Tdim = kmax + p;
-    const int64_t bstride = D * (int64_t)ncols;
+    const int64_t bmax = D * (int64_t)S0 * p;
     Launcher<T> L{op, st, &res.launches};
-    const Geo g = make_geo(D, ncols);
-    const int kcap = std::max(Tdim, K);
+    const int kcap = Tdim;
+    int nch_max = 0, nchu_max = 0;
+    for (int S = 1; S <= S0; ++S) {
+        nch_max = std::max(nch_max, make_geo(D, S * p).nchunks);
+        nchu_max = std::max(nchu_max, make_ugeo(D, S * p).nchunks);
+    }
 
-    DevBuf<T> Va((size_t)(nb + 1) * bstride), Vb((size_t)(nb + 1) * bstride), W((size_t)bstride);
-    DevBuf<double> part((size_t)g.nchunks * kcap * ncols), gpart((size_t)g.nchunks * p * ncols);
-    DevBuf<T> Cf((size_t)kcap * ncols);
-    DevBuf<double> Rinv((size_t)S * p * p), Tm((size_t)S * Tdim * Tdim), scale(S);
-    DevBuf<int> brk(S);
-    DevBuf<T> Yd((size_t)S * kmax * kmax);
-    BH_CUDA(cudaMemcpyAsync(scale.p, d_scale_init, S * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    // Va: basis (nb blocks + residual block).  Vb: restart target, and scratch
+    // for the CholQR2 intermediate while a segment runs.
+    DevBuf<T> Va((size_t)(nb + 1) * bmax), Vb((size_t)(nb + 1) * bmax), W((size_t)bmax);
+    DevBuf<double> part((size_t)nch_max * kcap * S0 * p), gpart((size_t)nchu_max * p * S0 * p);
+    DevBuf<T> Cf((size_t)kcap * S0 * p);
+    DevBuf<double> Rinv((size_t)S0 * p * p), Racc((size_t)S0 * p * p), Tm((size_t)S0 * Tdim * Tdim),
+        d_prm((size_t)3 * S0);
+    DevBuf<unsigned char> dead((size_t)S0 * Tdim);
+    DevBuf<int> d_in(S0), d_out(S0);
+    DevBuf<T> Yd((size_t)S0 * kmax * kmax);
+    Xout.alloc((size_t)D * S0 * K);
+    theta_out.assign((size_t)S0 * K, 0.0);
+    res.nconv.assign(S0, 0);
+    res.conv_at.assign(S0, -1);
+    res.scale.assign(S0, 1.0);
+
+    std::vector<int> act(S0);  // original index of each active solve
+    std::iota(act.begin(), act.end(), 0);
+    int S = S0;
+    auto upload_prm = [&]() {
+        std::vector<double> pr((size_t)3 * S);
+        for (int a = 0; a < S; ++a)
+            for (int k = 0; k < 3; ++k) pr[3 * a + k] = prm_all[3 * act[a] + k];
+        BH_CUDA(cudaMemcpyAsync(d_prm.p, pr.data(), pr.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+        BH_CUDA(cudaStreamSynchronize(st));  // host vector goes out of scope
+    };
+    upload_prm();
     BH_CUDA(cudaMemsetAsync(Tm.p, 0, Tm.bytes(), st));
-    std::vector<int> hbrk(S, -1);
-    BH_CUDA(cudaMemcpyAsync(brk.p, hbrk.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
-    const double eps_t = std::is_same<T, float>::value ? 1.1920929e-7 : 2.220446049250313e-16;
-    const double rel_tiny = 1e3 * eps_t;
+    BH_CUDA(cudaMemsetAsync(dead.p, 0, dead.bytes(), st));
+    const bool fp32 = std::is_same<T, float>::value;
+    // shifted first pass: cond(W R0^{-1})^2 <= 1 / shift_rel, small enough for
+    // two plain Cholesky QR passes in this precision
+    const double shift_rel = fp32 ? 1e3 * 1.1920929e-7 : 1e3 * 2.220446049250313e-16;
+    // a direction is dropped only at rounding-noise level
+    const double kill_abs = fp32 ? 3.0 * 1.1920929e-7 : 1e2 * 2.220446049250313e-16;
+
+    // orthonormalise the block W into Vout (scratch: Vb); T coupling written for jrow > 0
+    auto orthonormalize = [&](const Geo& gu, int ncols, T* Wb, T* Vout, int jrow, bool gram_done) {
+        T* scratch = Vb.p;
+        double* Tj = jrow > 0 ? Tm.p : nullptr;
+        if (!gram_done) L.update(gu, p, 0, 0, Va.p, Cf.p, Wb, 1, gpart.p);
+        if (p == 1) {
+            L.qr(gu, S, p, gpart.p, 2, 0.0, Racc.p, Rinv.p, Tj, Tdim, jrow, kill_abs, dead.p);
+            L.normalize(ncols, p, Rinv.p, Wb, Vout);
+            return;
+        }
+        // shifted CholQR3: Wb -> scratch -> Wb -> Vout
+        L.qr(gu, S, p, gpart.p, 0, shift_rel, Racc.p, Rinv.p, nullptr, Tdim, jrow, kill_abs, nullptr);
+        L.normalize(ncols, p, Rinv.p, Wb, scratch);
+        L.update(gu, p, 0, 0, Va.p, Cf.p, scratch, 1, gpart.p);
+        L.qr(gu, S, p, gpart.p, 1, 0.0, Racc.p, Rinv.p, nullptr, Tdim, jrow, kill_abs, nullptr);
+        L.normalize(ncols, p, Rinv.p, scratch, Wb);
+        L.update(gu, p, 0, 0, Va.p, Cf.p, Wb, 1, gpart.p);
+        L.qr(gu, S, p, gpart.p, 2, 0.0, Racc.p, Rinv.p, Tj, Tdim, jrow, kill_abs, dead.p);
+        L.normalize(ncols, p, Rinv.p, Wb, Vout);
+    };
 
     // start block: W = seeded stream; V_1 = H W (Spectra forces v into range(A)); V_0 = QR(V_1)
-    k_start_block<T><<<elem_grid(bstride), 256, 0, st>>>(D, ncols, p, rq.seed, rq.d_perm, W.p);
-    BH_CUDA(cudaGetLastError());
-    ++res.launches;
-    T* V1 = Va.p + bstride;
-    L.spmm(ncols, p, d_prm, W.p, V1);
-    res.matvecs += p;
-    L.update(g, p, 0, bstride, Va.p, Cf.p, V1, 1, gpart.p);
-    L.qr(g, S, p, gpart.p, Rinv.p, nullptr, Tdim, 0, nullptr, 0.0, nullptr);
-    L.normalize(ncols, p, Rinv.p, V1, Va.p);
+    {
+        const int ncols = S * p;
+        const int64_t bstride = D * ncols;
+        k_start_block<T><<<elem_grid(bstride), 256, 0, st>>>(D, ncols, p, rq.seed, rq.d_perm, W.p);
+        BH_CUDA(cudaGetLastError());
+        ++res.launches;
+        T* V1 = Va.p + bstride;
+        L.spmm(ncols, p, d_prm.p, W.p, V1);
+        res.matvecs += p;
+        const Geo gu0 = make_ugeo(D, ncols);
+        orthonormalize(gu0, ncols, V1, Va.p, 0, false);
+        // H W can lose rank (H singular on the seeded block, e.g. the
+        // one-state sector with H = 0): then start from the seeded block itself
+        std::vector<double> hr((size_t)S * p * p);
+        BH_CUDA(cudaMemcpyAsync(hr.data(), Racc.p, hr.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+        BH_CUDA(cudaStreamSynchronize(st));
+        bool degenerate = false;
+        for (int a = 0; a < S; ++a)
+            for (int q = 0; q < p; ++q) degenerate |= !(hr[(size_t)a * p * p + q * p + q] != 0.0);
+        if (degenerate) orthonormalize(gu0, ncols, W.p, Va.p, 0, false);
+    }
 
-    std::vector<double> hT((size_t)S * Tdim * Tdim);
-    std::vector<double> theta((size_t)S * kmax), Yh((size_t)S * kmax * kmax), resid((size_t)S * kmax);
-    std::vector<int> kuse(S, kmax);
+    std::vector<double> hT, theta((size_t)S0 * kmax), Yh((size_t)S0 * kmax * kmax), resid((size_t)S0 * kmax);
+    std::vector<unsigned char> hdead;
+    std::vector<int> kuse(S0, kmax);
     std::vector<T> Yt;
-    res.conv_at.assign(S, -1);
-    res.scale.assign(S, 1.0);
     int jstart = 0;
+    bool after_restart = false;
     int restarts = 0;
     const double eps23 = std::pow(2.220446049250313e-16, 2.0 / 3.0);
     for (;;) {
+        const int ncols = S * p;
+        const int64_t bstride = D * ncols;
+        const Geo g = make_geo(D, ncols), gu = make_ugeo(D, ncols);
         for (int j = jstart; j < nb; ++j) {
             T* Vj = Va.p + (int64_t)j * bstride;
-            L.spmm(ncols, p, d_prm, Vj, W.p);
+            L.spmm(ncols, p, d_prm.p, Vj, W.p);
             res.matvecs += p;
+            // local step: A = V_j^T W, then W -= V_j A + earlier couplings
+            const int c_lo = (j == jstart && after_restart) ? 0 : std::max(0, (j - 1) * p);
+            L.dot(g, ncols, p, 1, bstride, Vj, W.p, kcap, part.p);
+            L.local_coef(g, j, c_lo, p, kcap, part.p, Tm.p, Tdim, Cf.p);
+            L.update(gu, p, (j + 1) * p - c_lo, bstride, Va.p + (int64_t)(c_lo / p) * bstride, Cf.p,
+                     W.p, 0, gpart.p);
+            // one full re-orthogonalisation pass, Gram matrix of the result
             const int kc = (j + 1) * p;
-            for (int pass = 0; pass < 2; ++pass) {
-                L.dot(g, ncols, p, j + 1, bstride, Va.p, W.p, kcap, part.p);
-                L.dot_finalize(g, kc, ncols, p, kcap, part.p, nullptr, Cf.p, Tm.p, Tdim, j);
-                L.update(g, p, kc, bstride, Va.p, Cf.p, W.p, pass == 1, gpart.p);
-            }
-            L.qr(g, S, p, gpart.p, Rinv.p, Tm.p, Tdim, j + 1, scale.p, rel_tiny, brk.p);
-            L.normalize(ncols, p, Rinv.p, W.p, Va.p + (int64_t)(j + 1) * bstride);
+            L.dot(g, ncols, p, j + 1, bstride, Va.p, W.p, kcap, part.p);
+            L.dot_finalize(g, kc, ncols, p, kcap, part.p, nullptr, Cf.p, Tm.p, Tdim, j);
+            L.update(gu, p, kc, bstride, Va.p, Cf.p, W.p, 1, gpart.p);
+            orthonormalize(gu, ncols, W.p, Va.p + (int64_t)(j + 1) * bstride, j + 1, true);
         }
+        if (debug_ortho()) {
+            // Gram matrix of all nb + 1 blocks against each block, solve 0
+            double worst = 0.0;
+            std::vector<double> hc((size_t)(kmax + p) * ncols);
+            DevBuf<double> dC((size_t)(kmax + p) * ncols);
+            for (int jb = 0; jb <= nb; ++jb) {
+                L.dot(g, ncols, p, nb + 1, bstride, Va.p, Va.p + (int64_t)jb * bstride, kcap, part.p);
+                L.dot_finalize(g, kmax + p, ncols, p, kcap, part.p, dC.p, nullptr, nullptr, 0, 0);
+                BH_CUDA(cudaMemcpyAsync(hc.data(), dC.p, hc.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+                BH_CUDA(cudaStreamSynchronize(st));
+                for (int c = 0; c < kmax + p; ++c)
+                    for (int q = 0; q < p; ++q) {
+                        const double want = (c == jb * p + q) ? 1.0 : 0.0;
+                        worst = std::max(worst, std::fabs(hc[(size_t)c * ncols + q] - want));
+                    }
+            }
+            std::fprintf(stderr, "[bh] restart %d: solve %d basis max|V^T V - I| = %.3e\n", restarts, act[0], worst);
+        }
+        hT.resize((size_t)S * Tdim * Tdim);
+        hdead.resize((size_t)S * Tdim);
         BH_CUDA(cudaMemcpyAsync(hT.data(), Tm.p, hT.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-        BH_CUDA(cudaMemcpyAsync(hbrk.data(), brk.p, S * sizeof(int), cudaMemcpyDeviceToHost, st));
+        BH_CUDA(cudaMemcpyAsync(hdead.data(), dead.p, hdead.size(), cudaMemcpyDeviceToHost, st));
         BH_CUDA(cudaStreamSynchronize(st));
 
-        // Rayleigh-Ritz per solve (host, FP64)
+        // Rayleigh-Ritz per active solve (host, FP64) on the live columns of T
         std::vector<int> nconv(S, 0);
         std::vector<double> hscale(S, 1.0);
         bool symeig_failed = false;
-        parallel_for(S, [&](int s) {
-            const double* Ts = hT.data() + (size_t)s * Tdim * Tdim;
-            int k = kmax;
-            if (hbrk[s] >= 0) k = std::min(k, hbrk[s] * p);
-            kuse[s] = k;
-            std::vector<double> a((size_t)k * k), w(k);
+        parallel_for(S, [&](int a) {
+            const double* Ts = hT.data() + (size_t)a * Tdim * Tdim;
+            const unsigned char* dd = hdead.data() + (size_t)a * Tdim;
+            std::vector<int> live;
+            for (int c = 0; c < kmax; ++c)
+                if (!dd[c]) live.push_back(c);
+            const int k = (int)live.size();
+            kuse[a] = k;
+            std::vector<double> m((size_t)k * k), w(k);
             for (int jj = 0; jj < k; ++jj)
                 for (int ii = 0; ii < k; ++ii) {
-                    const int lo = std::min(ii, jj), hi = std::max(ii, jj);
-                    a[(size_t)jj * k + ii] = Ts[(size_t)hi * Tdim + lo];  // upper triangle
+                    const int lo = std::min(live[ii], live[jj]), hi = std::max(live[ii], live[jj]);
+                    m[(size_t)jj * k + ii] = Ts[(size_t)hi * Tdim + lo];  // upper triangle
                 }
-            if (!symeig(k, a.data(), w.data())) symeig_failed = true;
+            if (!symeig(k, m.data(), w.data())) symeig_failed = true;
             double sc = 0.0;
             for (int i = 0; i < k; ++i) sc = std::max(sc, std::fabs(w[i]));
-            hscale[s] = std::max(sc, 1e-300);
+            hscale[a] = std::max(sc, 1e-300);
+            for (int i = 0; i < kmax; ++i)
+                for (int c = 0; c < kmax; ++c) Yh[((size_t)a * kmax + c) * kmax + i] = 0.0;
             for (int i = 0; i < k; ++i) {
-                theta[(size_t)s * kmax + i] = w[i];
-                for (int c = 0; c < k; ++c) Yh[((size_t)s * kmax + c) * kmax + i] = a[(size_t)i * k + c];
+                theta[(size_t)a * kmax + i] = w[i];
+                for (int ii = 0; ii < k; ++ii) Yh[((size_t)a * kmax + live[ii]) * kmax + i] = m[(size_t)i * k + ii];
                 double r2 = 0.0;
-                if (k == kmax && hbrk[s] < 0) {
-                    for (int a2 = 0; a2 < p; ++a2) {
-                        double v = 0.0;
-                        for (int b2 = 0; b2 < p; ++b2)
-                            v += Ts[(size_t)(kmax - p + b2) * Tdim + kmax + a2] * a[(size_t)i * k + kmax - p + b2];
-                        r2 += v * v;
-                    }
+                for (int a2 = 0; a2 < p; ++a2) {
+                    double v = 0.0;
+                    for (int b2 = 0; b2 < p; ++b2)
+                        v += Ts[(size_t)(kmax - p + b2) * Tdim + kmax + a2] *
+                             Yh[((size_t)a * kmax + kmax - p + b2) * kmax + i];
+                    r2 += v * v;
                 }
-                resid[(size_t)s * kmax + i] = std::sqrt(r2);
+                resid[(size_t)a * kmax + i] = std::sqrt(r2);
             }
             // Convergence: resid <= tol * max(|theta|, floor).  Spectra uses
             // floor = eps^(2/3); a residual estimate built from the computed
-            // projection cannot fall below ~eps * ||H||, so the floor here is a
-            // fraction of the spectral radius estimate (largest |Ritz value|).
+            // projection cannot fall below ~eps * ||H||, so the floor here is
+            // a fraction of the spectral radius estimate (largest |Ritz value|).
             int nc = 0;
-            const double floor_abs = rq.precision == BH_PREC_MIXED ? hscale[s] : std::max(eps23, 1e-3 * hscale[s]);
+            const double floor_abs = rq.precision == BH_PREC_MIXED ? hscale[a] : std::max(eps23, 1e-3 * hscale[a]);
             for (int i = 0; i < std::min(rq.nev, k); ++i) {
                 const double th = std::fabs(w[i]);
-                if (resid[(size_t)s * kmax + i] <= rq.tol * std::max(th, floor_abs)) ++nc;
+                if (resid[(size_t)a * kmax + i] <= rq.tol * std::max(th, floor_abs)) ++nc;
             }
-            nconv[s] = nc;
+            nconv[a] = nc;
         });
         if (symeig_failed) throw Error(BH_ERR_NOCONV, "projected eigenproblem did not converge");
-        res.scale = hscale;
-        bool done = true;
-        int minconv = rq.nev, nact = 0;
-        for (int s = 0; s < S; ++s) {
-            if (kuse[s] < rq.nev) throw Error(BH_ERR_BREAKDOWN, "Krylov space exhausted before nev eigenvalues (dimension too small or invariant start block)");
-            const bool conv_s = nconv[s] >= rq.nev || hbrk[s] >= 0;
-            if (!conv_s) {
-                done = false;
-                ++nact;
-            }
-            if (conv_s && res.conv_at[s] < 0) res.conv_at[s] = restarts;
-            minconv = std::min(minconv, nconv[s]);
+        const bool last = restarts >= rq.max_restarts;
+        std::vector<int> fin, cont;  // active positions
+        int minconv = rq.nev, ndead = 0;
+        for (int a = 0; a < S; ++a) {
+            if (kuse[a] < rq.nev)
+                throw Error(BH_ERR_BREAKDOWN, "Krylov space exhausted before nev eigenvalues (dimension too small or invariant start block)");
+            const int o = act[a];
+            res.nconv[o] = nconv[a];
+            res.scale[o] = hscale[a];
+            ndead += kmax - kuse[a];
+            const bool conv_a = nconv[a] >= rq.nev;
+            if (conv_a && res.conv_at[o] < 0) res.conv_at[o] = restarts;
+            if (conv_a || last) fin.push_back(a);
+            else cont.push_back(a);
+            minconv = std::min(minconv, nconv[a]);
         }
-        res.nconv.assign(nconv.begin(), nconv.end());
         if (verbose()) {
             double worst = 0.0;
-            for (int s = 0; s < S; ++s)
-                for (int i = 0; i < rq.nev && i < kuse[s]; ++i) {
-                    const double floor_abs = rq.precision == BH_PREC_MIXED ? hscale[s] : std::max(eps23, 1e-3 * hscale[s]);
-                    worst = std::max(worst, resid[(size_t)s * kmax + i] / std::max(std::fabs(theta[(size_t)s * kmax + i]), floor_abs));
+            for (int a = 0; a < S; ++a)
+                for (int i = 0; i < rq.nev && i < kuse[a]; ++i) {
+                    const double floor_abs = rq.precision == BH_PREC_MIXED ? hscale[a] : std::max(eps23, 1e-3 * hscale[a]);
+                    worst = std::max(worst, resid[(size_t)a * kmax + i] / std::max(std::fabs(theta[(size_t)a * kmax + i]), floor_abs));
                 }
-            std::fprintf(stderr, "[bh] restart %d: unconverged solves %d/%d, min nconv %d, worst rel resid %.3e\n",
-                         restarts, nact, S, minconv, worst);
+            std::fprintf(stderr, "[bh] restart %d: active %d, retiring %d, min nconv %d, dropped dirs %d, worst rel resid %.3e\n",
+                         restarts, S, (int)fin.size(), minconv, ndead, worst);
+            for (int a : fin) {
+                std::fprintf(stderr, "[bh]   retire solve %d: live %d theta0 %.10f resid:", act[a], kuse[a],
+                             theta[(size_t)a * kmax]);
+                for (int i = 0; i < rq.nev && i < kuse[a]; ++i) std::fprintf(stderr, " %.1e", resid[(size_t)a * kmax + i]);
+                std::fprintf(stderr, "\n");
+            }
         }
-        if (done || restarts >= rq.max_restarts) break;
 
-        // thick restart: keep the nkeep lowest Ritz vectors + the residual block
+        // retire finished solves: their K lowest Ritz vectors go to Xout[:, orig K + i]
+        if (!fin.empty()) {
+            const int nf = (int)fin.size();
+            Yt.assign((size_t)nf * kmax * K, T(0));
+            std::vector<int> in(nf), out(nf);
+            for (int f = 0; f < nf; ++f) {
+                const int a = fin[f], o = act[a];
+                in[f] = a;
+                out[f] = o;
+                for (int i = 0; i < K; ++i) {
+                    theta_out[(size_t)o * K + i] = i < kuse[a] ? theta[(size_t)a * kmax + i] : 0.0;
+                    for (int c = 0; c < kmax; ++c)
+                        Yt[((size_t)f * kmax + c) * K + i] = i < kuse[a] ? (T)Yh[((size_t)a * kmax + c) * kmax + i] : T(0);
+                }
+            }
+            BH_CUDA(cudaMemcpyAsync(Yd.p, Yt.data(), Yt.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+            BH_CUDA(cudaMemcpyAsync(d_in.p, in.data(), nf * sizeof(int), cudaMemcpyHostToDevice, st));
+            BH_CUDA(cudaMemcpyAsync(d_out.p, out.data(), nf * sizeof(int), cudaMemcpyHostToDevice, st));
+            L.rotate(nf, ncols, p, kmax, K, bstride, Va.p, Yd.p, d_in.p, d_out.p, Xout.p, 0, S0 * K, 1);
+            BH_CUDA(cudaStreamSynchronize(st));
+        }
+        if (cont.empty()) break;
+
+        // thick restart of the continuing solves, compacted to the front
         int nkeep = rq.nev + std::max(p, (kmax - rq.nev) / 2);
         nkeep = (nkeep + p - 1) / p * p;
         nkeep = std::min(nkeep, kmax - 2 * p);
         if (nkeep < p) nkeep = p;
-        Yt.assign((size_t)S * kmax * nkeep, T(0));
-        for (int s = 0; s < S; ++s)
+        for (int a : cont) nkeep = std::min(nkeep, kuse[a] / p * p);
+        const int nc = (int)cont.size();
+        const int ncols2 = nc * p;
+        const int64_t bstride2 = D * ncols2;
+        Yt.assign((size_t)nc * kmax * nkeep, T(0));
+        std::vector<int> in(nc), out(nc);
+        for (int f = 0; f < nc; ++f) {
+            const int a = cont[f];
+            in[f] = a;
+            out[f] = f;
             for (int c = 0; c < kmax; ++c)
                 for (int i = 0; i < nkeep; ++i)
-                    Yt[((size_t)s * kmax + c) * nkeep + i] = (T)Yh[((size_t)s * kmax + c) * kmax + i];
+                    Yt[((size_t)f * kmax + c) * nkeep + i] = (T)Yh[((size_t)a * kmax + c) * kmax + i];
+        }
         BH_CUDA(cudaMemcpyAsync(Yd.p, Yt.data(), Yt.size() * sizeof(T), cudaMemcpyHostToDevice, st));
-        L.rotate(S, ncols, p, kmax, nkeep, bstride, Va.p, Yd.p, Vb.p, bstride, 0);
-        BH_CUDA(cudaMemcpyAsync(Vb.p + (int64_t)(nkeep / p) * bstride, Va.p + (int64_t)nb * bstride,
-                                bstride * sizeof(T), cudaMemcpyDeviceToDevice, st));
+        BH_CUDA(cudaMemcpyAsync(d_in.p, in.data(), nc * sizeof(int), cudaMemcpyHostToDevice, st));
+        BH_CUDA(cudaMemcpyAsync(d_out.p, out.data(), nc * sizeof(int), cudaMemcpyHostToDevice, st));
+        L.rotate(nc, ncols, p, kmax, nkeep, bstride, Va.p, Yd.p, d_in.p, d_out.p, Vb.p, bstride2, ncols2, 0);
+        L.gather_block(nc, p, ncols, ncols2, d_in.p, Va.p + (int64_t)nb * bstride,
+                       Vb.p + (int64_t)(nkeep / p) * bstride2);
         std::swap(Va.p, Vb.p);  // equal sizes: ownership stays balanced
-        // new projected matrix: diag(theta_keep) plus the coupling rows
-        //   T[nkeep + a][i] = sum_b R_last[a][b] Y[kmax - p + b][i]
-        // (the upper arrowhead is recomputed by the next expansion step)
-        std::vector<double> hTn(hT.size(), 0.0);
-        for (int s = 0; s < S; ++s) {
-            const double* To = hT.data() + (size_t)s * Tdim * Tdim;
-            double* Ts = hTn.data() + (size_t)s * Tdim * Tdim;
-            for (int i = 0; i < nkeep; ++i) Ts[(size_t)i * Tdim + i] = theta[(size_t)s * kmax + i];
-            for (int a = 0; a < p; ++a)
+        if (debug_ortho()) {
+            // orthonormality of the rotated basis (nkeep/p + 1 blocks), solve 0
+            const Geo g2 = make_geo(D, ncols2);
+            const int nbk = nkeep / p + 1;
+            double worst = 0.0;
+            std::vector<double> hc((size_t)nbk * p * ncols2);
+            DevBuf<double> dC((size_t)nbk * p * ncols2);
+            for (int jb = 0; jb < nbk; ++jb) {
+                L.dot(g2, ncols2, p, nbk, bstride2, Va.p, Va.p + (int64_t)jb * bstride2, kcap, part.p);
+                L.dot_finalize(g2, nbk * p, ncols2, p, kcap, part.p, dC.p, nullptr, nullptr, 0, 0);
+                BH_CUDA(cudaMemcpyAsync(hc.data(), dC.p, hc.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+                BH_CUDA(cudaStreamSynchronize(st));
+                for (int c = 0; c < nbk * p; ++c)
+                    for (int q = 0; q < p; ++q) {
+                        const double want = (c == jb * p + q) ? 1.0 : 0.0;
+                        worst = std::max(worst, std::fabs(hc[(size_t)c * ncols2 + q] - want));
+                    }
+            }
+            std::fprintf(stderr, "[bh] restart %d: rotated basis max|V^T V - I| = %.3e (nkeep %d)\n", restarts, worst, nkeep);
+        }
+        // projected matrix of the continuing solves: diag(theta_keep) plus the
+        // coupling rows  T[nkeep + a][i] = sum_b R_last[a][b] Y[kmax - p + b][i]
+        // (the upper arrowhead is filled by the next local step); the dropped
+        // flags of the residual block move with it
+        std::vector<double> hTn((size_t)nc * Tdim * Tdim, 0.0);
+        std::vector<unsigned char> hdn((size_t)nc * Tdim, 0);
+        for (int f = 0; f < nc; ++f) {
+            const int a = cont[f];
+            const double* To = hT.data() + (size_t)a * Tdim * Tdim;
+            double* Ts = hTn.data() + (size_t)f * Tdim * Tdim;
+            for (int i = 0; i < nkeep; ++i) Ts[(size_t)i * Tdim + i] = theta[(size_t)a * kmax + i];
+            for (int a2 = 0; a2 < p; ++a2) {
+                hdn[(size_t)f * Tdim + nkeep + a2] = hdead[(size_t)a * Tdim + kmax + a2];
                 for (int i = 0; i < nkeep; ++i) {
                     double v = 0.0;
                     for (int b = 0; b < p; ++b)
-                        v += To[(size_t)(kmax - p + b) * Tdim + kmax + a] *
-                             Yh[((size_t)s * kmax + kmax - p + b) * kmax + i];
-                    Ts[(size_t)i * Tdim + nkeep + a] = v;
+                        v += To[(size_t)(kmax - p + b) * Tdim + kmax + a2] *
+                             Yh[((size_t)a * kmax + kmax - p + b) * kmax + i];
+                    Ts[(size_t)i * Tdim + nkeep + a2] = v;
                 }
+            }
         }
-        hT.swap(hTn);
-        BH_CUDA(cudaMemcpyAsync(Tm.p, hT.data(), hT.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-        BH_CUDA(cudaMemcpyAsync(scale.p, hscale.data(), S * sizeof(double), cudaMemcpyHostToDevice, st));
+        std::vector<int> act2(nc);
+        for (int f = 0; f < nc; ++f) act2[f] = act[cont[f]];
+        act.swap(act2);
+        S = nc;
+        BH_CUDA(cudaMemcpyAsync(Tm.p, hTn.data(), hTn.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+        BH_CUDA(cudaMemcpyAsync(dead.p, hdn.data(), hdn.size(), cudaMemcpyHostToDevice, st));
+        upload_prm();
         jstart = nkeep / p;
+        after_restart = true;
         ++restarts;
     }
     res.restarts = restarts;
-
-    // Ritz vectors of the K lowest values: X[r][s K + i]
-    Yt.assign((size_t)S * kmax * K, T(0));
-    theta_out.assign((size_t)S * K, 0.0);
-    for (int s = 0; s < S; ++s) {
-        const int k = kuse[s];
-        for (int i = 0; i < K; ++i) {
-            theta_out[(size_t)s * K + i] = i < k ? theta[(size_t)s * kmax + i] : 0.0;
-            for (int c = 0; c < k; ++c)
-                Yt[((size_t)s * kmax + c) * K + i] = i < k ? (T)Yh[((size_t)s * kmax + c) * kmax + i] : T(0);
-        }
-    }
-    BH_CUDA(cudaMemcpyAsync(Yd.p, Yt.data(), Yt.size() * sizeof(T), cudaMemcpyHostToDevice, st));
-    Xout.alloc((size_t)D * S * K);
-    L.rotate(S, ncols, p, kmax, K, bstride, Va.p, Yd.p, Xout.p, 0, S * K);
     BH_CUDA(cudaStreamSynchronize(st));
-    // Va/Vb swapped raw pointers above: keep ownership consistent
 }
 
 void apply_operator(const OpView<double>& op, int ncols, int group, const double* d_prm,
@@ -865,22 +1210,21 @@ SolveResult block_lanczos(const OpView<double>& op64, const OpView<float>& op32,
     BH_REQUIRE(S >= 1 && p >= 1 && p <= 16 && (p & (p - 1)) == 0, "block size must be 1, 2, 4, 8 or 16");
     BH_REQUIRE(rq.nev >= 1 && rq.nev <= 32, "nev must be in [1, 32]");
     BH_REQUIRE((int64_t)S * p <= 512, "batch too wide: S * block must be <= 512");
-    BH_REQUIRE(rq.kmax % p == 0 && rq.kmax >= rq.nev + p, "ncv must be a multiple of the block size and >= nev + block");
+    BH_REQUIRE(rq.kmax % p == 0 && (rq.kmax >= rq.nev + p || (rq.kmax == D && rq.kmax >= rq.nev)),
+               "ncv must be a multiple of the block size and >= nev + block (or the whole space)");
     BH_REQUIRE((int64_t)rq.kmax <= D, "ncv exceeds the dimension");
     const int K = (rq.nev + p - 1) / p * p;  // Ritz vectors refined in FP64
     BH_REQUIRE(K <= 32 && K <= rq.kmax, "too many wanted eigenvalues for this block size");
 
     // per-solve parameters (J, U, shift) and start scale
-    std::vector<double> prm((size_t)3 * S), sc(S, 1.0);
+    std::vector<double> prm((size_t)3 * S);
     for (int s = 0; s < S; ++s) {
         prm[3 * s] = rq.J[s];
         prm[3 * s + 1] = rq.U[s];
         prm[3 * s + 2] = rq.shift[s];
-        sc[s] = std::fabs(rq.J[s]) + std::fabs(rq.U[s]) + std::fabs(rq.shift[s]) + 1e-300;
     }
-    DevBuf<double> d_prm(prm.size()), d_sc(S);
+    DevBuf<double> d_prm(prm.size());
     BH_CUDA(cudaMemcpyAsync(d_prm.p, prm.data(), prm.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-    BH_CUDA(cudaMemcpyAsync(d_sc.p, sc.data(), S * sizeof(double), cudaMemcpyHostToDevice, st));
 
     // ---- Lanczos phase ----
     DevBuf<double> X64;
@@ -888,14 +1232,14 @@ SolveResult block_lanczos(const OpView<double>& op64, const OpView<float>& op32,
     if (rq.precision == BH_PREC_MIXED) {
         BH_REQUIRE(op32.tv != nullptr, "mixed precision needs FP32 operator values");
         DevBuf<float> X32;
-        lanczos_phase<float>(op32, rq, d_prm.p, d_sc.p, st, res, K, X32, theta0);
+        lanczos_phase<float>(op32, rq, prm, st, res, K, X32, theta0);
         X64.alloc((size_t)D * S * K);
         k_convert<float, double><<<elem_grid(D * S * K), 256, 0, st>>>(D * S * K, X32.p, X64.p);
         BH_CUDA(cudaGetLastError());
         ++res.launches;
         BH_CUDA(cudaStreamSynchronize(st));
     } else {
-        lanczos_phase<double>(op64, rq, d_prm.p, d_sc.p, st, res, K, X64, theta0);
+        lanczos_phase<double>(op64, rq, prm, st, res, K, X64, theta0);
     }
 
     // ---- FP64 Rayleigh-Ritz refinement on the K Ritz vectors per solve ----
@@ -990,9 +1334,14 @@ SolveResult block_lanczos(const OpView<double>& op64, const OpView<float>& op32,
     std::vector<double> hrn(nc2);
     BH_CUDA(cudaMemcpyAsync(hrn.data(), rn.p, nc2 * sizeof(double), cudaMemcpyDeviceToHost, st));
     DevBuf<double> Xf;
+    DevBuf<int> d_id;
     if (rq.want_vectors) {
+        std::vector<int> id(S);
+        std::iota(id.begin(), id.end(), 0);
+        d_id.alloc(S);
+        BH_CUDA(cudaMemcpyAsync(d_id.p, id.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
         Xf.alloc((size_t)D * nc2);
-        L.rotate(S, nc2, K, K, K, 0, X64.p, d_Z.p, Xf.p, 0, nc2);
+        L.rotate(S, nc2, K, K, K, 0, X64.p, d_Z.p, d_id.p, d_id.p, Xf.p, 0, nc2, 1);
     }
     BH_CUDA(cudaStreamSynchronize(st));
 
@@ -1007,9 +1356,11 @@ SolveResult block_lanczos(const OpView<double>& op64, const OpView<float>& op32,
             const double fl = std::max(eps23, 1e-3 * res.scale[s]);
             res.resid[(size_t)s * nev + i] = std::sqrt(std::max(0.0, hrn[(size_t)s * K + i])) / std::max(std::fabs(e), fl);
         }
+    profile_flush();
     if (rq.want_vectors) {
         std::vector<double> hx((size_t)D * nc2);
-        BH_CUDA(cudaMemcpy(hx.data(), Xf.p, hx.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        BH_CUDA(cudaMemcpyAsync(hx.data(), Xf.p, hx.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+        BH_CUDA(cudaStreamSynchronize(st));
         res.vecs.assign((size_t)S * nev * D, 0.0);
         for (int64_t r = 0; r < D; ++r)
             for (int s = 0; s < S; ++s)

@@ -14,6 +14,7 @@ struct OpView {
     const T* tv = nullptr;
     const T* vd = nullptr;
     int64_t D = 0;
+    int64_t rp_nnz = 0;  // stored entries (for the algorithmic byte count)
 };
 
 struct SolveRequest {

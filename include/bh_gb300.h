@@ -140,6 +140,7 @@ typedef struct bh_solve_info {
     int64_t matvecs;   /* H x products per solve                                  */
     double max_resid;  /* max relative residual of the returned pairs             */
     double seconds;    /* wall time of the call                                   */
+    int64_t launches;  /* kernels launched by the call                            */
 } bh_solve_info;
 
 void bh_solver_opts_default(bh_solver_opts* o);
@@ -188,6 +189,21 @@ int bh_spdm(const bh_hamiltonian* h, int order, const double* phi, double* rho);
  * (central differences, one-sided at the ends of the mu grid). */
 int bh_phase_map(int m, int n_lo, int nsec, int nJ, const double* e0, int nmu, const double* mu,
                  double* density, double* compressibility);
+
+/* ---------------------------------------------------------------------- */
+/* Tracing (no counterpart in the reference beyond Resource::timer,        */
+/* src/resource.cpp:55-71): per-kernel device time from CUDA events.       */
+/* ---------------------------------------------------------------------- */
+
+/* Turns per-kernel event timing on or off (process-wide; off by default). */
+int bh_profile_enable(int on);
+/* Clears the accumulated totals. */
+int bh_profile_reset(void);
+/* Number of distinct kernels with totals. */
+int bh_profile_count(int* n);
+/* Totals of kernel i: name, launches, device milliseconds and algorithmic
+ * bytes (every operand read once and every result written once). */
+int bh_profile_get(int i, char* name, int name_cap, int64_t* launches, double* ms, double* bytes);
 
 #ifdef __cplusplus
 }

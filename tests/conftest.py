@@ -68,3 +68,10 @@ def oracle_H(orc, m, n, lists, order="reference"):
         rp, ci, tv = orc.build_T(occ, off, flat)
         vd = orc.diag_V(occ)
     return occ, col_of_lex, lex_of_col, rp, ci, tv, vd
+
+
+def reference_lowest(rec):
+    """The reference's lowest nev eigenvalues with multiplicity: its run with
+    nev + 2 wanted values (see tests/golden/make_golden.py), else its nev run."""
+    v = rec.get("evals_lowest_from_nev_plus_2") or rec["evals_sorted"]
+    return v
