@@ -56,7 +56,7 @@ EXPORTS = [
     "bh_basis_info", "bh_basis_copy", "bh_basis_index", "bh_hamiltonian_create",
     "bh_hamiltonian_destroy", "bh_hamiltonian_nnz", "bh_hamiltonian_csr",
     "bh_hamiltonian_apply", "bh_solver_opts_default", "bh_eigsh", "bh_eigsh_csr",
-    "bh_eigsh_batch", "bh_gap_ratios", "bh_spdm", "bh_phase_map", "bh_profile_enable",
+    "bh_eigsh_batch", "bh_dense_eigh", "bh_gap_ratios", "bh_spdm", "bh_phase_map", "bh_profile_enable",
     "bh_profile_reset", "bh_profile_count", "bh_profile_get",
 ]
 
@@ -98,6 +98,7 @@ def load() -> C.CDLL:
                                C.POINTER(bh_solve_info)]
     L.bh_eigsh_batch.argtypes = [vp, C.c_int, vp, vp, vp, C.POINTER(bh_solver_opts), vp, vp, vp,
                                  C.POINTER(bh_solve_info)]
+    L.bh_dense_eigh.argtypes = [C.c_int64, vp, vp, vp]
     L.bh_gap_ratios.argtypes = [C.c_int, vp, vp, f64p]
     L.bh_spdm.argtypes = [vp, C.c_int, vp, vp]
     L.bh_phase_map.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, vp, C.c_int, vp, vp, vp]
@@ -404,6 +405,19 @@ class Op:
 # ---------------------------------------------------------------------------
 # Analysis namespace mirror (analysis.hpp)
 # ---------------------------------------------------------------------------
+def exact_eigen(O):
+    """Op::exact_eigen: all eigenvalues (ascending) and eigenvectors (columns)."""
+    A = np.asfortranarray(O.toarray() if hasattr(O, "toarray") else np.asarray(O), dtype=np.float64)
+    n = A.shape[0]
+    w = np.zeros(n)
+    z = np.zeros((n, n), order="F")
+    _check(load().bh_dense_eigh(n, _ptr(A), _ptr(w), z.ctypes.data_as(C.c_void_p)))
+    return w, z
+
+
+Op.exact_eigen = staticmethod(exact_eigen)
+
+
 class Analysis:
     @staticmethod
     def gap_ratios(eigenvalues, nb_eigen: int) -> np.ndarray:

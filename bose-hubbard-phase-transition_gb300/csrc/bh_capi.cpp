@@ -441,6 +441,13 @@ int bh_eigsh_csr(int64_t dim, const int64_t* row_ptr, const int32_t* col, const 
     });
 }
 
+int bh_dense_eigh(int64_t n, const double* a, double* w, double* z) {
+    return guard([&] {
+        BH_REQUIRE(a && w, "null argument");
+        dense_eigh(n, a, w, z);
+    });
+}
+
 // ---- observables ----
 int bh_gap_ratios(int nev, const double* evals, double* ratios, double* mean) {
     return guard([&] {

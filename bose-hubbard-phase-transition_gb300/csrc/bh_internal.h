@@ -157,6 +157,10 @@ Lists square_lists(int m, bool closed);
 Lists cube_lists(int m, bool closed);
 void flatten(const Lists& nb, int32_t* off, int32_t* out, int cap, int* count);
 
+// ---- dense symmetric eigensolver on the device (bh_dense.cu) ----
+// a: n x n column-major (host); w: eigenvalues ascending; z (optional): vectors
+void dense_eigh(int64_t n, const double* h_a, double* h_w, double* h_z);
+
 // ---- optional per-kernel timing (bh_profile.cpp) ----
 bool profile_on();
 void profile_begin(cudaStream_t st);

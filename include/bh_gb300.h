@@ -168,6 +168,11 @@ int bh_eigsh_batch(const bh_hamiltonian* h, int nsolve, const double* J, const d
                    const double* mu, const bh_solver_opts* o, double* evals, double* resid,
                    int* nconv, bh_solve_info* info);
 
+/* Replaces Op::exact_eigen (operator.cpp:92-101): all eigenvalues (ascending)
+ * and, if z != NULL, eigenvectors (columns of z, column-major n x n) of the
+ * dense symmetric matrix a (column-major, host).  n <= 32768. */
+int bh_dense_eigh(int64_t n, const double* a, double* w, double* z);
+
 /* ---------------------------------------------------------------------- */
 /* Observables                                                             */
 /* ---------------------------------------------------------------------- */
