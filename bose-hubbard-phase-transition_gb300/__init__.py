@@ -55,7 +55,7 @@ EXPORTS = [
     "bh_neighbours_cube", "bh_dimension", "bh_basis_create", "bh_basis_destroy",
     "bh_basis_info", "bh_basis_copy", "bh_basis_index", "bh_hamiltonian_create",
     "bh_hamiltonian_destroy", "bh_hamiltonian_nnz", "bh_hamiltonian_csr",
-    "bh_hamiltonian_apply", "bh_solver_opts_default", "bh_eigsh", "bh_eigsh_csr",
+    "bh_hamiltonian_apply", "bh_hamiltonian_apply_noalloc", "bh_solver_opts_default", "bh_eigsh", "bh_eigsh_csr",
     "bh_eigsh_batch", "bh_dense_eigh", "bh_gap_ratios", "bh_spdm", "bh_phase_map", "bh_profile_enable",
     "bh_profile_reset", "bh_profile_count", "bh_profile_get",
 ]
@@ -90,6 +90,8 @@ def load() -> C.CDLL:
     L.bh_hamiltonian_nnz.argtypes = [vp, i64p]
     L.bh_hamiltonian_csr.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, vp, vp, vp]
     L.bh_hamiltonian_apply.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, vp, vp]
+    L.bh_hamiltonian_apply_noalloc.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double,
+                                                C.c_int, vp, vp, vp]
     L.bh_solver_opts_default.argtypes = [C.POINTER(bh_solver_opts)]
     L.bh_solver_opts_default.restype = None
     L.bh_eigsh.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.POINTER(bh_solver_opts),

@@ -1202,6 +1202,25 @@ void apply_operator(const OpView<double>& op, int ncols, int group, const double
     L.spmm(ncols, group, d_prm, d_X, d_Y);
 }
 
+// Same product, launched with no profiling events and no host allocation.
+void apply_operator_raw(const OpView<double>& op, int ncols, int group, const double* d_prm,
+                        const double* d_X, double* d_Y, cudaStream_t st) {
+    int L = 1;
+    while (L < 32 && L * 2 <= ncols && ncols % (L * 2) == 0) L *= 2;
+    const int rpb = 256 / L;
+    int64_t g = (op.D + rpb - 1) / rpb;
+    g = std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)sm_count() * 16));
+    switch (L) {
+        case 1: k_spmm<double, 1><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, d_prm, d_X, d_Y); break;
+        case 2: k_spmm<double, 2><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, d_prm, d_X, d_Y); break;
+        case 4: k_spmm<double, 4><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, d_prm, d_X, d_Y); break;
+        case 8: k_spmm<double, 8><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, d_prm, d_X, d_Y); break;
+        case 16: k_spmm<double, 16><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, d_prm, d_X, d_Y); break;
+        default: k_spmm<double, 32><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, d_prm, d_X, d_Y); break;
+    }
+    BH_CUDA(cudaGetLastError());
+}
+
 SolveResult block_lanczos(const OpView<double>& op64, const OpView<float>& op32,
                           const SolveRequest& rq, cudaStream_t st) {
     SolveResult res;

@@ -48,6 +48,10 @@ struct SolveResult {
 void apply_operator(const OpView<double>& op, int ncols, int group, const double* d_prm,
                     const double* d_X, double* d_Y, cudaStream_t st);
 
+// The same product with no profiling events and no allocation.
+void apply_operator_raw(const OpView<double>& op, int ncols, int group, const double* d_prm,
+                        const double* d_X, double* d_Y, cudaStream_t st);
+
 // op64 must be set; op32 must be set for BH_PREC_MIXED (same pattern).
 SolveResult block_lanczos(const OpView<double>& op64, const OpView<float>& op32,
                           const SolveRequest& rq, cudaStream_t st);

@@ -117,6 +117,22 @@ int bh_hamiltonian_csr(const bh_hamiltonian* h, int order, double J, double U, d
 /* y = H x for nvec vectors (x, y: host, row-major [D][nvec], `order`). */
 int bh_hamiltonian_apply(const bh_hamiltonian* h, int order, double J, double U, double mu,
                          int nvec, const double* x, double* y);
+/* No counterpart in the reference.  y = H x like bh_hamiltonian_apply, for
+ * callers that cannot allocate device memory while they run (a host
+ * application that hands out device memory once from its own pool, or many
+ * host threads sharing one GPU, where cudaMalloc/cudaFree serialise against
+ * all other device work): x and y are DEVICE pointers [D][nvec] in `order`,
+ * the work is queued on `stream` (a cudaStream_t, NULL = legacy default
+ * stream) and the call returns when it has finished.  It allocates nothing:
+ * its working memory is a fixed 32 MiB device array inside the library
+ * (4 Mi doubles), shared by all calls and kept by every GPU that loads the
+ * library until exit, so 2 * D * nvec must not exceed 4 Mi - 32 doubles in
+ * the reference order (BH_ERR_ARG otherwise; the lexicographic order needs no
+ * vector scratch).  The first call on each device looks up that array's
+ * device address and should come before any stream capture.  Calls that
+ * overlap on the GPU race on the shared array: serialise them. */
+int bh_hamiltonian_apply_noalloc(const bh_hamiltonian* h, int order, double J, double U,
+                                 double mu, int nvec, const double* x, double* y, void* stream);
 
 /* ---------------------------------------------------------------------- */
 /* Eigensolver                                                             */
