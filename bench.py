@@ -329,6 +329,8 @@ def run_ours(args):
                            "algorithmic_bytes_per_launch": round(per_launch_bytes)}
         out["kernel_time_shares"] = {k: round(v["ms"] / tot_ms, 4)
                                      for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])}
+        out["kernel_gbs"] = {k: round(v["bytes"] / (v["ms"] * 1e6), 1)
+                             for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"]) if v["ms"] > 0}
 
         rate, cores, secs = cpu_sample_rate()
         out["cpu_baseline"] = {"value": round(rate, 4), "unit": "eigensolves/s", "cores": cores,

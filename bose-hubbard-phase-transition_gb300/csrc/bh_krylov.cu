@@ -29,6 +29,7 @@
 // the returned eigenvalues and their true FP64 residuals.
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <numeric>
@@ -148,16 +149,31 @@ k_dot(int64_t D, int ncols, int ld, int p, int nblk, int64_t bstride, const T* _
     }
 }
 
-// C = sum over chunks; Cf = (T)C; optionally T_s[c][jcol p + q'] += C
+// Sum of one coefficient's chunk partials by one warp (lanes stride over the
+// chunks, then a fixed-order shuffle tree): the result is deterministic.
+__device__ __forceinline__ double warp_sum_chunks(const double* __restrict__ part, int nchunks,
+                                                  size_t chunk_stride, size_t offset) {
+    const int lane = threadIdx.x & 31;
+    double v = 0.0;
+#pragma unroll 4
+    for (int ch = lane; ch < nchunks; ch += 32) v += part[(size_t)ch * chunk_stride + offset];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// C = sum over chunks; Cf = (T)C; optionally T_s[c][jcol p + q'] += C.
+// One warp per coefficient.
 template <class T>
 __global__ void k_dot_finalize(int nchunks, int kc, int ncols, int ldC, int p, int kcap,
                                const double* __restrict__ part, double* __restrict__ C,
                                T* __restrict__ Cf, double* __restrict__ Tm, int Tdim, int jcol) {
     const int total = kc * ncols;
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < total; idx += warps) {
         const int c = idx / ncols, t = idx % ncols;
-        double sum = 0.0;
-        for (int ch = 0; ch < nchunks; ++ch) sum += part[((size_t)ch * kcap + c) * ncols + t];
+        const double sum = warp_sum_chunks(part, nchunks, (size_t)kcap * ncols, (size_t)c * ncols + t);
+        if ((threadIdx.x & 31) != 0) continue;
         if (C) C[(size_t)c * ldC + t] = sum;
         if (Cf) Cf[(size_t)c * ldC + t] = (T)sum;
         if (Tm) {
@@ -181,18 +197,18 @@ __global__ void k_local_coef(int nchunks, int j, int c_lo, int ncols, int p, int
                              T* __restrict__ Cf) {
     const int rows = (j + 1) * p - c_lo;
     const int total = rows * ncols;
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int idx = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; idx < total; idx += warps) {
         const int cr = idx / ncols, t = idx % ncols;
         const int c = c_lo + cr;
         const int s = t / p, q = t % p;
         double* Ts = Tm + (size_t)s * Tdim * Tdim;
         double v;
-        if (c >= j * p) {
-            v = 0.0;
-            for (int ch = 0; ch < nchunks; ++ch) v += part[((size_t)ch * kcap + (c - j * p)) * ncols + t];
-        } else {
+        if (c >= j * p)
+            v = warp_sum_chunks(part, nchunks, (size_t)kcap * ncols, (size_t)(c - j * p) * ncols + t);
+        else
             v = Ts[(size_t)c * Tdim + j * p + q];
-        }
+        if ((threadIdx.x & 31) != 0) continue;
         Cf[(size_t)cr * ncols + t] = (T)v;
         Ts[(size_t)(j * p + q) * Tdim + c] += v;
     }
@@ -298,6 +314,270 @@ k_update(int64_t D, int ncols, int p, int lp, int kc, int64_t bstride, const T* 
     }
 }
 
+// ---- per-solve vector kernels for block sizes P = 1, 2, 4 ----
+// A thread owns all P columns of one solve in a row: loads are P-wide vectors
+// (a warp reads 32 solves x P contiguous values), and the P x P products of a
+// block need no data from other lanes.
+template <class T, int P>
+struct Vec {
+    T v[P];
+};
+
+template <class T, int P>
+__device__ __forceinline__ Vec<T, P> ldv(const T* __restrict__ p) {
+    Vec<T, P> o;
+    if constexpr (P == 1) {
+        o.v[0] = p[0];
+    } else if constexpr (std::is_same<T, float>::value && P == 2) {
+        const float2 x = *reinterpret_cast<const float2*>(p);
+        o.v[0] = x.x;
+        o.v[1] = x.y;
+    } else if constexpr (std::is_same<T, float>::value && P == 4) {
+        const float4 x = *reinterpret_cast<const float4*>(p);
+        o.v[0] = x.x;
+        o.v[1] = x.y;
+        o.v[2] = x.z;
+        o.v[3] = x.w;
+    } else {
+#pragma unroll
+        for (int q = 0; q < P; q += 2) {
+            const double2 x = *reinterpret_cast<const double2*>(p + q);
+            o.v[q] = x.x;
+            o.v[q + 1] = x.y;
+        }
+    }
+    return o;
+}
+
+template <class T, int P>
+__device__ __forceinline__ void stv(T* __restrict__ p, const Vec<T, P>& o) {
+    if constexpr (P == 1) {
+        p[0] = o.v[0];
+    } else if constexpr (std::is_same<T, float>::value && P == 2) {
+        *reinterpret_cast<float2*>(p) = make_float2(o.v[0], o.v[1]);
+    } else if constexpr (std::is_same<T, float>::value && P == 4) {
+        *reinterpret_cast<float4*>(p) = make_float4(o.v[0], o.v[1], o.v[2], o.v[3]);
+    } else {
+#pragma unroll
+        for (int q = 0; q < P; q += 2) *reinterpret_cast<double2*>(p + q) = make_double2(o.v[q], o.v[q + 1]);
+    }
+}
+
+// Partial sums of C_s[(j P + q)][q'] = sum_r V_j[r][s P + q] W[r][s P + q']
+// over one chunk of rows (blockIdx.y) and JT blocks (tile blockIdx.x: the
+// tiles of one chunk run side by side, so W's chunk is read from DRAM once).
+// Thread = (solve s, row group ro); the loads of RU rows (JT + 1 vectors
+// each) are issued before their products.  Products are summed in T per
+// thread and flushed every 32 rows into the thread's own FP64 slots in shared
+// memory (s_red[val NT + tid]), which the CTA then sums over the row groups
+// in a fixed order.  part layout as k_dot.
+template <class T, int P, int JT, int RU>
+__global__ void __launch_bounds__(128)
+k_dotv(int64_t D, int S, int nblk, int64_t bstride, const T* __restrict__ V,
+       const T* __restrict__ W, int64_t rows_per_chunk, int kcap, double* __restrict__ part) {
+    extern __shared__ double s_red[];
+    constexpr int NV = JT * P * P;
+    const int NT = blockDim.x;
+    const int ncols = S * P;
+    const int s = threadIdx.x % S, ro = threadIdx.x / S, R = NT / S;
+    const int64_t r0 = (int64_t)blockIdx.y * rows_per_chunk;
+    const int64_t r1 = min(D, r0 + rows_per_chunk);
+    const int j0 = blockIdx.x * JT;
+    const int nj = min(JT, nblk - j0);
+    double* mine = s_red + threadIdx.x;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) mine[(size_t)v * NT] = 0.0;
+    T acc[JT][P][P];
+#pragma unroll
+    for (int a = 0; a < JT; ++a)
+#pragma unroll
+        for (int q = 0; q < P; ++q)
+#pragma unroll
+            for (int b = 0; b < P; ++b) acc[a][q][b] = T(0);
+    const T* Vb = V + (int64_t)j0 * bstride + s * P;
+    const T* Wb = W + s * P;
+    int cnt = 0;
+    for (int64_t base = r0 + ro; base < r1; base += RU * R) {
+        Vec<T, P> w[RU], x[RU][JT];
+#pragma unroll
+        for (int u = 0; u < RU; ++u) {
+            const int64_t r = base + (int64_t)u * R;
+            const int64_t rr = r < r1 ? r : base;  // a valid row; its products are dropped
+            w[u] = ldv<T, P>(Wb + rr * ncols);
+#pragma unroll
+            for (int a = 0; a < JT; ++a)
+                if (a < nj) x[u][a] = ldv<T, P>(Vb + (int64_t)a * bstride + rr * ncols);
+            if (r >= r1)
+#pragma unroll
+                for (int b = 0; b < P; ++b) w[u].v[b] = T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < RU; ++u)
+#pragma unroll
+            for (int a = 0; a < JT; ++a)
+                if (a < nj)
+#pragma unroll
+                    for (int q = 0; q < P; ++q)
+#pragma unroll
+                        for (int b = 0; b < P; ++b) acc[a][q][b] += x[u][a].v[q] * w[u].v[b];
+        cnt += RU;
+        if (cnt >= 32) {
+            cnt = 0;
+#pragma unroll
+            for (int a = 0; a < JT; ++a)
+#pragma unroll
+                for (int q = 0; q < P; ++q)
+#pragma unroll
+                    for (int b = 0; b < P; ++b) {
+                        mine[(size_t)((a * P + q) * P + b) * NT] += (double)acc[a][q][b];
+                        acc[a][q][b] = T(0);
+                    }
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < JT; ++a)
+#pragma unroll
+        for (int q = 0; q < P; ++q)
+#pragma unroll
+            for (int b = 0; b < P; ++b) mine[(size_t)((a * P + q) * P + b) * NT] += (double)acc[a][q][b];
+    __syncthreads();
+    // one thread per (value, solve) sums the R row groups in order
+    for (int e = threadIdx.x; e < NV * S; e += NT) {
+        const int val = e / S, ss = e % S;
+        const int a = val / (P * P), q = (val / P) % P, b = val % P;
+        if (a >= nj) continue;
+        double sum = 0.0;
+        for (int u = 0; u < R; ++u) sum += s_red[(size_t)val * NT + u * S + ss];
+        part[((size_t)blockIdx.y * kcap + (size_t)(j0 + a) * P + q) * ncols + ss * P + b] = sum;
+    }
+}
+
+// W[r][s P + q'] -= sum_{c < kc} V_{c/P}[r][s P + c%P] Cf[c][s P + q'], then
+// (optionally) Gram partials G_s[q][q'] = sum_r W[r][s P + q] W[r][s P + q']
+// written as gpart[(cta P + q) ncols + s P + q'] (the k_update layout).
+// Two rows per iteration; the inner step issues the loads of several basis
+// blocks before using them.
+template <class T, int P>
+__global__ void __launch_bounds__(256)
+k_updatev(int64_t D, int S, int nblk, int64_t bstride, const T* __restrict__ V,
+          const T* __restrict__ Cf, T* __restrict__ W, int64_t rows_per_cta, int do_gram,
+          double* __restrict__ gpart) {
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    const int ncols = S * P;
+    const int kc = nblk * P;
+    T* sC = reinterpret_cast<T*>(s_raw);
+    double* sG = reinterpret_cast<double*>(s_raw + (((size_t)kc * ncols * sizeof(T) + 15) & ~(size_t)15));
+    for (int i = threadIdx.x; i < kc * ncols; i += blockDim.x) sC[i] = Cf[i];
+    __syncthreads();
+    const int s = threadIdx.x % S, ro = threadIdx.x / S, R = blockDim.x / S;
+    const int64_t r0 = (int64_t)blockIdx.x * rows_per_cta;
+    const int64_t r1 = min(D, r0 + rows_per_cta);
+    double gd[P][P];
+    T gf[P][P];
+#pragma unroll
+    for (int q = 0; q < P; ++q)
+#pragma unroll
+        for (int b = 0; b < P; ++b) {
+            gd[q][b] = 0.0;
+            gf[q][b] = T(0);
+        }
+    int cnt = 0;
+    const T* Vs = V + s * P;
+    for (int64_t base = r0; base < r1; base += 2 * R) {
+        const int64_t rA = base + ro, rB = rA + R;
+        const bool vA = rA < r1, vB = rB < r1;
+        Vec<T, P> wA, wB;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            wA.v[q] = T(0);
+            wB.v[q] = T(0);
+        }
+        if (vA) wA = ldv<T, P>(W + rA * ncols + s * P);
+        if (vB) wB = ldv<T, P>(W + rB * ncols + s * P);
+        if (nblk > 0 && vA) {
+            const T* pA = Vs + rA * ncols;
+            const T* pB = Vs + (vB ? rB : rA) * ncols;
+            T aA[P], aB[P];
+#pragma unroll
+            for (int q = 0; q < P; ++q) {
+                aA[q] = T(0);
+                aB[q] = T(0);
+            }
+            constexpr int U = P >= 4 ? 2 : 4;  // blocks per inner step: 2 U vector loads in flight
+            int j = 0;
+            for (; j + U - 1 < nblk; j += U) {
+                Vec<T, P> x[U], y[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    x[u] = ldv<T, P>(pA + (int64_t)(j + u) * bstride);
+                    y[u] = ldv<T, P>(pB + (int64_t)(j + u) * bstride);
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+#pragma unroll
+                    for (int q = 0; q < P; ++q) {
+                        const Vec<T, P> c = ldv<T, P>(sC + (size_t)((j + u) * P + q) * ncols + s * P);
+#pragma unroll
+                        for (int b = 0; b < P; ++b) {
+                            aA[b] += x[u].v[q] * c.v[b];
+                            aB[b] += y[u].v[q] * c.v[b];
+                        }
+                    }
+            }
+            for (; j < nblk; ++j) {
+                const Vec<T, P> x0 = ldv<T, P>(pA + (int64_t)j * bstride);
+                const Vec<T, P> y0 = ldv<T, P>(pB + (int64_t)j * bstride);
+#pragma unroll
+                for (int q = 0; q < P; ++q) {
+                    const Vec<T, P> c = ldv<T, P>(sC + (size_t)(j * P + q) * ncols + s * P);
+#pragma unroll
+                    for (int b = 0; b < P; ++b) {
+                        aA[b] += x0.v[q] * c.v[b];
+                        aB[b] += y0.v[q] * c.v[b];
+                    }
+                }
+            }
+#pragma unroll
+            for (int b = 0; b < P; ++b) {
+                wA.v[b] -= aA[b];
+                wB.v[b] = vB ? wB.v[b] - aB[b] : T(0);
+            }
+            stv<T, P>(W + rA * ncols + s * P, wA);
+            if (vB) stv<T, P>(W + rB * ncols + s * P, wB);
+        }
+        if (do_gram) {
+#pragma unroll
+            for (int q = 0; q < P; ++q)
+#pragma unroll
+                for (int b = 0; b < P; ++b) gf[q][b] += wA.v[q] * wA.v[b] + wB.v[q] * wB.v[b];
+            if (++cnt == 16) {
+                cnt = 0;
+#pragma unroll
+                for (int q = 0; q < P; ++q)
+#pragma unroll
+                    for (int b = 0; b < P; ++b) {
+                        gd[q][b] += (double)gf[q][b];
+                        gf[q][b] = T(0);
+                    }
+            }
+        }
+    }
+    if (do_gram) {
+#pragma unroll
+        for (int q = 0; q < P; ++q)
+#pragma unroll
+            for (int b = 0; b < P; ++b) sG[(size_t)(q * P + b) * blockDim.x + threadIdx.x] = gd[q][b] + (double)gf[q][b];
+        __syncthreads();
+        for (int e = threadIdx.x; e < P * P * S; e += blockDim.x) {
+            const int val = e / S, ss = e % S;
+            const int q = val / P, b = val % P;
+            double sum = 0.0;
+            for (int u = 0; u < R; ++u) sum += sG[(size_t)val * blockDim.x + u * S + ss];
+            gpart[((size_t)blockIdx.x * P + q) * ncols + ss * P + b] = sum;
+        }
+    }
+}
+
 // One CTA per solve: G = sum of the Gram partials (fixed-order tree
 // reduction), then one pass of the block orthonormalisation W = Q R:
 //   mode 0  shifted Cholesky  G + s I = R^T R, s = shift_rel * max_i G_ii,
@@ -319,23 +599,15 @@ k_qr_finalize(int p, int nchunks, int ncols, const double* __restrict__ gpart, i
               double shift_rel, double* __restrict__ Racc, double* __restrict__ Rinv,
               double* __restrict__ Tm, int Tdim, int jrow, double kill_abs,
               unsigned char* __restrict__ dead) {
-    __shared__ double red[QR_THREADS];
     __shared__ double G[16][16];
     const int s = blockIdx.x;
-    for (int e = 0; e < p * p; ++e) {
+    const int warp = threadIdx.x >> 5;
+    for (int e = warp; e < p * p; e += QR_THREADS / 32) {
         const int a = e / p, b = e % p;
-        double v = 0.0;
-        for (int ch = threadIdx.x; ch < nchunks; ch += QR_THREADS)
-            v += gpart[((size_t)ch * p + a) * ncols + s * p + b];
-        red[threadIdx.x] = v;
-        __syncthreads();
-        for (int off = QR_THREADS / 2; off > 0; off >>= 1) {
-            if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) G[a][b] = red[0];
-        __syncthreads();
+        const double v = warp_sum_chunks(gpart, nchunks, (size_t)p * ncols, (size_t)a * ncols + s * p + b);
+        if ((threadIdx.x & 31) == 0) G[a][b] = v;
     }
+    __syncthreads();
     if (threadIdx.x != 0) return;
     double R[16][16], Ri[16][16], Rt[16][16];
     for (int a = 0; a < p; ++a)
@@ -432,58 +704,198 @@ __global__ void k_normalize(int64_t D, int ncols, int p, const double* __restric
     }
 }
 
+// CholQR passes without materialised intermediates: w = W[r][s P ..] times
+// the nR upper-triangular factors Rinv_k (k < nR, slot k at Rinv + k rstride,
+// solve s at s P P, entry [b][q] at b P + q), each applied in T exactly as a
+// separate normalisation would; Vout (if not null) receives the result, and
+// with do_gram the Gram partials of the result go to gpart in the k_update
+// layout.  Four rows per iteration keep four loads in flight per thread.
+template <class T, int P>
+__global__ void __launch_bounds__(256)
+k_normgram(int64_t D, int S, int nR, const double* __restrict__ Rinv, int64_t rstride,
+           const T* __restrict__ W, T* __restrict__ Vout, int64_t rows_per_cta, int do_gram,
+           double* __restrict__ gpart) {
+    extern __shared__ double sG[];
+    constexpr int RU = 4;
+    const int ncols = S * P;
+    const int s = threadIdx.x % S, ro = threadIdx.x / S, R = blockDim.x / S;
+    T rm[3][P][P];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int b = 0; b < P; ++b)
+#pragma unroll
+            for (int q = 0; q < P; ++q)
+                rm[k][b][q] = k < nR ? (T)Rinv[(size_t)k * rstride + (size_t)s * P * P + b * P + q] : T(0);
+    const int64_t r0 = (int64_t)blockIdx.x * rows_per_cta;
+    const int64_t r1 = min(D, r0 + rows_per_cta);
+    double gd[P][P];
+    T gf[P][P];
+#pragma unroll
+    for (int q = 0; q < P; ++q)
+#pragma unroll
+        for (int b = 0; b < P; ++b) {
+            gd[q][b] = 0.0;
+            gf[q][b] = T(0);
+        }
+    int cnt = 0;
+    for (int64_t base = r0 + ro; base < r1; base += RU * R) {
+        Vec<T, P> w[RU];
+#pragma unroll
+        for (int u = 0; u < RU; ++u) {
+            const int64_t r = base + (int64_t)u * R;
+            if (r < r1) {
+                w[u] = ldv<T, P>(W + r * ncols + s * P);
+            } else {
+#pragma unroll
+                for (int q = 0; q < P; ++q) w[u].v[q] = T(0);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < RU; ++u) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                if (k < nR) {
+                    Vec<T, P> o;
+#pragma unroll
+                    for (int q = P - 1; q >= 0; --q) {
+                        T acc = T(0);
+#pragma unroll
+                        for (int b = 0; b <= q; ++b) acc += w[u].v[b] * rm[k][b][q];
+                        o.v[q] = acc;
+                    }
+                    w[u] = o;
+                }
+            }
+            const int64_t r = base + (int64_t)u * R;
+            if (Vout && r < r1) stv<T, P>(Vout + r * ncols + s * P, w[u]);
+            if (do_gram) {
+#pragma unroll
+                for (int q = 0; q < P; ++q)
+#pragma unroll
+                    for (int b = 0; b < P; ++b) gf[q][b] += w[u].v[q] * w[u].v[b];
+            }
+        }
+        if (do_gram && ++cnt == 8) {  // FP64 flush every 32 rows
+            cnt = 0;
+#pragma unroll
+            for (int q = 0; q < P; ++q)
+#pragma unroll
+                for (int b = 0; b < P; ++b) {
+                    gd[q][b] += (double)gf[q][b];
+                    gf[q][b] = T(0);
+                }
+        }
+    }
+    if (do_gram) {
+#pragma unroll
+        for (int q = 0; q < P; ++q)
+#pragma unroll
+            for (int b = 0; b < P; ++b) sG[(size_t)(q * P + b) * blockDim.x + threadIdx.x] = gd[q][b] + (double)gf[q][b];
+        __syncthreads();
+        for (int e = threadIdx.x; e < P * P * S; e += blockDim.x) {
+            const int val = e / S, ss = e % S;
+            const int q = val / P, b = val % P;
+            double sum = 0.0;
+            for (int u = 0; u < R; ++u) sum += sG[(size_t)val * blockDim.x + u * S + ss];
+            gpart[((size_t)blockIdx.x * P + q) * ncols + ss * P + b] = sum;
+        }
+    }
+}
+
 // Ritz rotation: for the processed solves ls < Sproc (input solve in_idx[ls],
 // output slot out_idx[ls]):  out[:, i] = sum_{c < kc} V[:, c] Y_ls[c][i].
 // Input column c of solve s is V_{c/p}[r][s p + c%p] (row stride ld_in).
 // Output: blocks of p columns  Vout[i/p][r][o p + i%p]  (block stride
 // ostride, row stride ld_out), or with single != 0 one row-major array
-// Vout[r][o nout + i].  Each thread owns one (solve, column-in-block) lane
-// of one row and produces its outputs eight at a time.
-template <class T>
+// Vout[r][o nout + i].
+// A CTA takes Sg solves (their Y in shared memory, rows zero-padded to npad,
+// a multiple of NO, and solves ystride apart so that the Sg rows read together fall in different
+// banks) and a chunk of rows; thread = (solve ls = tid % Sg, row).  The Sg
+// solves of one row are adjacent in memory (one sector for Sg p = 32 B / T),
+// so a warp's loads cover whole sectors, and each Y row segment it reads is
+// shared by the 32 / Sg lanes of one solve (a broadcast).  NO outputs stay in
+// registers; more outputs take further passes over the inputs.  PV = p for
+// p in {1, 2, 4} (one vector load per basis block), else 0 (scalar loads).
+template <class T, int NO, int PV>
 __global__ void __launch_bounds__(256)
 k_rotate(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t bstride,
          const T* __restrict__ V, const T* __restrict__ Yg, const int* __restrict__ in_idx,
          const int* __restrict__ out_idx, T* __restrict__ Vout, int64_t ostride, int ld_out,
-         int single, int Sg, int ystride, int64_t rows_per_chunk) {
+         int single, int Sg, int npad, int ystride, int64_t rows_per_chunk) {
+    constexpr int V4 = 16 / sizeof(T);
     extern __shared__ __align__(16) unsigned char s_raw[];
     T* sY = reinterpret_cast<T*>(s_raw);
-    const int sg0 = blockIdx.y * Sg;
+    const int sg0 = blockIdx.x * Sg;
     const int nsg = min(Sg, Sproc - sg0);
-    for (int i = threadIdx.x; i < nsg * kc * nout; i += blockDim.x) {
-        const int ls = i / (kc * nout), e = i - ls * (kc * nout);
-        sY[(size_t)ls * ystride + e] = Yg[(size_t)(sg0 + ls) * kc * nout + e];
+    for (int i = threadIdx.x; i < nsg * kc * npad; i += blockDim.x) {
+        const int ls = i / (kc * npad), e = i - ls * (kc * npad);
+        const int c = e / npad, o = e - c * npad;
+        sY[(size_t)ls * ystride + e] = o < nout ? Yg[((size_t)(sg0 + ls) * kc + c) * nout + o] : T(0);
     }
     __syncthreads();
-    const int width = Sg * p;
-    const int tl = threadIdx.x % width, ro = threadIdx.x / width, R = blockDim.x / width;
-    const int ls = tl / p, qo = tl % p;
+    const int ls = threadIdx.x % Sg;
     if (ls >= nsg) return;
+    const int rstep = blockDim.x / Sg;
     const int sin = in_idx[sg0 + ls], sout = out_idx[sg0 + ls];
-    const int nob = nout / p;
-    const int64_t r0 = (int64_t)blockIdx.x * rows_per_chunk;
+    const int nblk = kc / p;
+    const int64_t r0 = (int64_t)blockIdx.y * rows_per_chunk;
     const int64_t r1 = min(D, r0 + rows_per_chunk);
     const T* ys = sY + (size_t)ls * ystride;
-    for (int64_t r = r0 + ro; r < r1; r += R) {
-        const T* vr = V + r * ld_in + sin * p;
-        for (int jo0 = 0; jo0 < nob; jo0 += 8) {
-            T acc[8];
+    for (int64_t r = r0 + threadIdx.x / Sg; r < r1; r += rstep) {
+        const T* vr = V + r * ld_in + (int64_t)sin * p;
+        for (int o0 = 0; o0 < nout; o0 += NO) {
+            T acc[NO];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) acc[u] = T(0);
-            for (int c = 0; c < kc; ++c) {
-                const T x = vr[(int64_t)(c / p) * bstride + c % p];
-                const T* yr = ys + (size_t)c * nout + qo + jo0 * p;
+            for (int u = 0; u < NO; ++u) acc[u] = T(0);
+            if constexpr (PV >= 1) {
+                constexpr int UJ = PV == 1 ? 8 : (PV == 2 ? 4 : 2);
+                for (int j = 0; j < nblk; j += UJ) {
+                    Vec<T, PV> x[UJ];
 #pragma unroll
-                for (int u = 0; u < 8; ++u)
-                    if (jo0 + u < nob) acc[u] += x * yr[u * p];
+                    for (int u = 0; u < UJ; ++u)
+                        if (j + u < nblk) x[u] = ldv<T, PV>(vr + (int64_t)(j + u) * bstride);
+#pragma unroll
+                    for (int u = 0; u < UJ; ++u) {
+                        if (j + u < nblk) {
+#pragma unroll
+                            for (int q = 0; q < PV; ++q) {
+                                const T* yc = ys + (size_t)((j + u) * PV + q) * npad + o0;
+#pragma unroll
+                                for (int o = 0; o < NO; o += V4) {
+                                    const Vec<T, V4> y = ldv<T, V4>(yc + o);
+#pragma unroll
+                                    for (int w = 0; w < V4; ++w) acc[o + w] += x[u].v[q] * y.v[w];
+                                }
+                            }
+                        }
+                    }
+                }
+            } else {
+                for (int c = 0; c < kc; ++c) {
+                    const T x = vr[(int64_t)(c / p) * bstride + c % p];
+                    const T* yc = ys + (size_t)c * npad + o0;
+#pragma unroll
+                    for (int o = 0; o < NO; o += V4) {
+                        const Vec<T, V4> y = ldv<T, V4>(yc + o);
+#pragma unroll
+                        for (int w = 0; w < V4; ++w) acc[o + w] += x * y.v[w];
+                    }
+                }
             }
+            const int no = min(NO, nout - o0);
+            if (single) {
+                T* dst = Vout + r * ld_out + (int64_t)sout * nout + o0;
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                if (jo0 + u < nob) {
-                    const int i = (jo0 + u) * p + qo;
-                    if (single)
-                        Vout[r * ld_out + (int64_t)sout * nout + i] = acc[u];
-                    else
-                        Vout[(int64_t)(jo0 + u) * ostride + r * ld_out + sout * p + qo] = acc[u];
+                for (int u = 0; u < NO; ++u)
+                    if (u < no) dst[u] = acc[u];
+            } else {
+#pragma unroll
+                for (int u = 0; u < NO; ++u) {
+                    if (u < no) {
+                        const int i = o0 + u;
+                        Vout[(int64_t)(i / p) * ostride + r * ld_out + (int64_t)sout * p + i % p] = acc[u];
+                    }
                 }
             }
         }
@@ -668,13 +1080,13 @@ static Geo make_geo(int64_t D, int ncols) {
     return g;
 }
 
-// geometry of k_update: many small CTAs (each handles >= 16 R rows)
+// geometry of k_update / k_normgram / k_qr_finalize: about 4 CTAs per SM
 static Geo make_ugeo(int64_t D, int ncols) {
     Geo g;
     g.ncols = ncols;
     g.R = std::max(1, 256 / ncols);
     g.NT = ncols * g.R;
-    const int64_t target = 16LL * sm_count();
+    const int64_t target = 4LL * sm_count();
     int64_t rpc = (D + target - 1) / target;
     rpc = std::max<int64_t>(rpc, (int64_t)g.R * 16);
     rpc = (rpc + 2 * g.R - 1) / (2 * g.R) * (2 * g.R);
@@ -734,10 +1146,45 @@ struct Launcher {
         if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         profile_begin(st);
         kern<<<grid, g.NT, smem, st>>>(op.D, g.ncols, ld, p, nblk, bstride, V, W, g.rows_per_chunk, kcap, part);
-        done("k_dot", (double)(nblk + 1) * op.D * g.ncols * sizeof(T));
+        done(nblk == 1 ? "k_dot(1 block)" : "k_dot", (double)(nblk + 1) * op.D * g.ncols * sizeof(T));
+    }
+    // per-solve vector path: P = p in {1, 2, 4}, packed rows, aligned P-vectors
+    bool vec_ok(int ld, int ncols, int p, int64_t bstride, const void* A, const void* B) const {
+        if (!(p == 1 || p == 2 || p == 4) || ld != ncols || ncols / p > 256) return false;
+        const uintptr_t al = (uintptr_t)p * sizeof(T);
+        return bstride % p == 0 && ((uintptr_t)A % al) == 0 && ((uintptr_t)B % al) == 0;  // null passes
+    }
+    template <int P, int JT, int RU>
+    void dotv_t(const Geo& g, int nblk, int64_t bstride, const T* V, const T* W, int kcap,
+                double* part) const {
+        const int S = g.ncols / P;
+        const int NT = S * std::max(1, 128 / S);  // small CTAs: several resident per SM
+        BH_REQUIRE(g.nchunks <= 65535, "too many row chunks for the reduction grid");
+        dim3 grid((nblk + JT - 1) / JT, g.nchunks);
+        const size_t smem = (size_t)NT * JT * P * P * sizeof(double);
+        auto kern = k_dotv<T, P, JT, RU>;
+        if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        profile_begin(st);
+        kern<<<grid, NT, smem, st>>>(op.D, S, nblk, bstride, V, W, g.rows_per_chunk, kcap, part);
+        done(nblk == 1 ? "k_dot(1 block)" : "k_dot", (double)(nblk + 1) * op.D * g.ncols * sizeof(T));
     }
     void dot(const Geo& g, int ld, int p, int nblk, int64_t bstride, const T* V, const T* W,
              int kcap, double* part) const {
+        if (vec_ok(ld, g.ncols, p, bstride, V, W)) {
+            // (JT blocks, RU rows) per step: 1 block and 4 rows for the local
+            // step, else 4 blocks (2 for P = 4) and 2 rows
+            if (p == 1) {
+                if (nblk == 1) dotv_t<1, 1, 4>(g, nblk, bstride, V, W, kcap, part);
+                else dotv_t<1, 8, 2>(g, nblk, bstride, V, W, kcap, part);
+            } else if (p == 2) {
+                if (nblk == 1) dotv_t<2, 1, 4>(g, nblk, bstride, V, W, kcap, part);
+                else dotv_t<2, 4, 2>(g, nblk, bstride, V, W, kcap, part);
+            } else {
+                if (nblk == 1) dotv_t<4, 1, 2>(g, nblk, bstride, V, W, kcap, part);
+                else dotv_t<4, 2, 2>(g, nblk, bstride, V, W, kcap, part);
+            }
+            return;
+        }
         if (p <= 1) dot_t<1>(g, ld, p, nblk, bstride, V, W, kcap, part);
         else if (p <= 2) dot_t<2>(g, ld, p, nblk, bstride, V, W, kcap, part);
         else if (p <= 4) dot_t<4>(g, ld, p, nblk, bstride, V, W, kcap, part);
@@ -748,7 +1195,7 @@ struct Launcher {
     void dot_finalize(const Geo& g, int kc, int ldC, int p, int kcap, const double* part, double* C,
                       T* Cf, double* Tm, int Tdim, int jcol) const {
         profile_begin(st);
-        k_dot_finalize<T><<<elem_grid((int64_t)kc * g.ncols), 256, 0, st>>>(
+        k_dot_finalize<T><<<elem_grid((int64_t)kc * g.ncols * 32), 256, 0, st>>>(
             g.nchunks, kc, g.ncols, ldC, p, kcap, part, C, Cf, Tm, Tdim, jcol);
         done("k_dot_finalize", (double)g.nchunks * kc * g.ncols * 8.0);
     }
@@ -756,13 +1203,13 @@ struct Launcher {
                     int Tdim, T* Cf) const {
         const int64_t total = (int64_t)((j + 1) * p - c_lo) * g.ncols;
         profile_begin(st);
-        k_local_coef<T><<<elem_grid(total), 256, 0, st>>>(g.nchunks, j, c_lo, g.ncols, p, kcap, part,
+        k_local_coef<T><<<elem_grid(total * 32), 256, 0, st>>>(g.nchunks, j, c_lo, g.ncols, p, kcap, part,
                                                           Tm, Tdim, Cf);
         done("k_local_coef", (double)g.nchunks * p * g.ncols * 8.0);
     }
     template <int PMAX>
     void update_t(const Geo& g, int p, int kc, int64_t bstride, const T* V, const T* Cf, T* W,
-                  int do_gram, double* gpart) const {
+                  int do_gram, double* gpart, const char* name) const {
         const size_t smem = (((size_t)kc * g.ncols * sizeof(T) + 15) & ~(size_t)15) +
                             (size_t)g.NT * PMAX * sizeof(double);
         if ((int)smem > max_smem_optin()) throw Error(BH_ERR_ARG, "Krylov basis too wide for shared memory (reduce ncv or batch)");
@@ -771,16 +1218,37 @@ struct Launcher {
         profile_begin(st);
         kern<<<g.nchunks, g.NT, smem, st>>>(op.D, g.ncols, p, ilog2(p), kc, bstride, V, Cf, W,
                                             g.rows_per_chunk, do_gram, gpart);
-        done(kc > 0 ? "k_update" : "k_update(gram)",
+        done(name ? name : (kc > 0 ? "k_update" : "k_update(gram)"),
+             (double)(kc > 0 ? kc + 2 : 1) * op.D * g.ncols * sizeof(T));
+    }
+    template <int P>
+    void updatev_t(const Geo& g, int kc, int64_t bstride, const T* V, const T* Cf, T* W, int do_gram,
+                   double* gpart, const char* name) const {
+        const int S = g.ncols / P;
+        const int NT = S * std::max(1, 256 / S);
+        const size_t smem = (((size_t)kc * g.ncols * sizeof(T) + 15) & ~(size_t)15) +
+                            (size_t)NT * P * P * sizeof(double);
+        if ((int)smem > max_smem_optin()) throw Error(BH_ERR_ARG, "Krylov basis too wide for shared memory (reduce ncv or batch)");
+        auto kern = k_updatev<T, P>;
+        if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        profile_begin(st);
+        kern<<<g.nchunks, NT, smem, st>>>(op.D, S, kc / P, bstride, V, Cf, W, g.rows_per_chunk, do_gram, gpart);
+        done(name ? name : (kc > 0 ? "k_update" : "k_update(gram)"),
              (double)(kc > 0 ? kc + 2 : 1) * op.D * g.ncols * sizeof(T));
     }
     void update(const Geo& g, int p, int kc, int64_t bstride, const T* V, const T* Cf, T* W,
-                int do_gram, double* gpart) const {
-        if (p <= 1) update_t<1>(g, p, kc, bstride, V, Cf, W, do_gram, gpart);
-        else if (p <= 2) update_t<2>(g, p, kc, bstride, V, Cf, W, do_gram, gpart);
-        else if (p <= 4) update_t<4>(g, p, kc, bstride, V, Cf, W, do_gram, gpart);
-        else if (p <= 8) update_t<8>(g, p, kc, bstride, V, Cf, W, do_gram, gpart);
-        else update_t<16>(g, p, kc, bstride, V, Cf, W, do_gram, gpart);
+                int do_gram, double* gpart, const char* name = nullptr) const {
+        if (kc % std::max(p, 1) == 0 && vec_ok(g.ncols, g.ncols, p, kc > 0 ? bstride : 0, kc > 0 ? V : W, W)) {
+            if (p == 1) updatev_t<1>(g, kc, bstride, V, Cf, W, do_gram, gpart, name);
+            else if (p == 2) updatev_t<2>(g, kc, bstride, V, Cf, W, do_gram, gpart, name);
+            else updatev_t<4>(g, kc, bstride, V, Cf, W, do_gram, gpart, name);
+            return;
+        }
+        if (p <= 1) update_t<1>(g, p, kc, bstride, V, Cf, W, do_gram, gpart, name);
+        else if (p <= 2) update_t<2>(g, p, kc, bstride, V, Cf, W, do_gram, gpart, name);
+        else if (p <= 4) update_t<4>(g, p, kc, bstride, V, Cf, W, do_gram, gpart, name);
+        else if (p <= 8) update_t<8>(g, p, kc, bstride, V, Cf, W, do_gram, gpart, name);
+        else update_t<16>(g, p, kc, bstride, V, Cf, W, do_gram, gpart, name);
     }
     void qr(const Geo& gu, int S, int p, const double* gpart, int mode, double shift_rel,
             double* Racc, double* Rinv, double* Tm, int Tdim, int jrow, double kill_abs,
@@ -789,6 +1257,25 @@ struct Launcher {
         k_qr_finalize<<<S, QR_THREADS, 0, st>>>(p, gu.nchunks, gu.ncols, gpart, mode, shift_rel, Racc,
                                                 Rinv, Tm, Tdim, jrow, kill_abs, dead);
         done("k_qr_finalize", (double)gu.nchunks * p * gu.ncols * 8.0);
+    }
+    template <int P>
+    void normgram_t(const Geo& g, int nR, const double* Rinv, int64_t rstride, const T* W, T* Vout,
+                    int do_gram, double* gpart) const {
+        const int S = g.ncols / P;
+        const int NT = S * std::max(1, 256 / S);
+        const size_t smem = do_gram ? (size_t)NT * P * P * sizeof(double) : 0;
+        auto kern = k_normgram<T, P>;
+        if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        profile_begin(st);
+        kern<<<g.nchunks, NT, smem, st>>>(op.D, S, nR, Rinv, rstride, W, Vout, g.rows_per_chunk, do_gram, gpart);
+        done(Vout ? "k_normalize" : "k_gram", (double)op.D * g.ncols * sizeof(T) * (Vout ? 2.0 : 1.0));
+    }
+    // nR factors applied to W; result to Vout (optional) and/or its Gram partials
+    void normgram(const Geo& g, int p, int nR, const double* Rinv, int64_t rstride, const T* W, T* Vout,
+                  int do_gram, double* gpart) const {
+        if (p == 1) normgram_t<1>(g, nR, Rinv, rstride, W, Vout, do_gram, gpart);
+        else if (p == 2) normgram_t<2>(g, nR, Rinv, rstride, W, Vout, do_gram, gpart);
+        else normgram_t<4>(g, nR, Rinv, rstride, W, Vout, do_gram, gpart);
     }
     void normalize(int ncols, int p, const double* Rinv, const T* W, T* Vout) const {
         profile_begin(st);
@@ -800,30 +1287,54 @@ struct Launcher {
                 const T* Yg, const int* in_idx, const int* out_idx, T* Vout, int64_t ostride,
                 int ld_out, int single) const {
         if (Sproc <= 0) return;
-        const int smax = std::min(max_smem_optin(), 160 * 1024);
-        const int ystride = (kc * nout) | 1;  // odd: solves land on different banks
+        constexpr int V4 = 16 / sizeof(T), E = 128 / sizeof(T);
+        // outputs per pass (a template value below); Y rows padded to a whole
+        // number of passes so that every pass reads inside its row
+        const int NO = sizeof(T) == 4 ? (nout <= 16 ? 16 : (nout <= 32 ? 32 : 48))
+                                      : (nout <= 8 ? 8 : (nout <= 16 ? 16 : 24));
+        const int npad = (nout + NO - 1) / NO * NO;
+        const int ystride = ((kc * npad + E - 1) / E) * E + V4;
         const size_t per = (size_t)ystride * sizeof(T);
+        const int smax = std::min(max_smem_optin(), 200 * 1024);
         if ((int)per > smax) throw Error(BH_ERR_ARG, "restart rotation too large for shared memory (reduce ncv)");
-        int Sg = (int)std::min<size_t>((size_t)Sproc, std::max<size_t>(1, (size_t)(64 * 1024) / per));
-        Sg = std::min(Sg, std::max(1, 128 / p));
-        while (Sg > 1 && 256 % (Sg * p) != 0) --Sg;
+        // Sg solves per CTA: one 32-byte sector per row when p and shared memory allow
+        int Sg = std::max(1, std::min(8, (int)(32 / ((size_t)p * sizeof(T)))));
+        Sg = std::min(Sg, std::max(1, (int)((size_t)smax / per)));
+        Sg = std::min(Sg, Sproc);
+        while (Sg > 1 && 256 % Sg != 0) --Sg;
         const size_t smem = (size_t)Sg * per;
-        const int width = Sg * p;
-        const int NT = std::max(width, 256 / width * width);
         const int ngroups = (Sproc + Sg - 1) / Sg;
-        const int R = NT / width;
-        int64_t chunks = std::max<int64_t>(1, (4LL * sm_count()) / ngroups);
+        const int rstep = 256 / Sg;
+        int64_t chunks = std::max<int64_t>(1, (6LL * sm_count() + ngroups - 1) / ngroups);
         int64_t rpc = (op.D + chunks - 1) / chunks;
-        rpc = std::max<int64_t>(rpc, 2LL * R);
+        rpc = std::max<int64_t>(rpc, rstep);
         chunks = (op.D + rpc - 1) / rpc;
+        BH_REQUIRE(chunks <= 65535, "too many row chunks for the rotation grid");
+        const bool vec = (p == 1 || p == 2 || p == 4) && ld_in % p == 0 && bstride % p == 0 &&
+                         ((uintptr_t)V % ((uintptr_t)p * sizeof(T))) == 0;
         auto launch = [&](auto kern) {
             if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            kern<<<dim3((unsigned)chunks, ngroups), NT, smem, st>>>(
+            kern<<<dim3((unsigned)ngroups, (unsigned)chunks), 256, smem, st>>>(
                 op.D, Sproc, ld_in, p, kc, nout, bstride, V, Yg, in_idx, out_idx, Vout, ostride,
-                ld_out, single, Sg, ystride, rpc);
+                ld_out, single, Sg, npad, ystride, rpc);
+        };
+        auto pick = [&](auto pv) {
+            constexpr int PV = decltype(pv)::value;
+            if constexpr (sizeof(T) == 4) {
+                if (NO == 16) launch(k_rotate<T, 16, PV>);
+                else if (NO == 32) launch(k_rotate<T, 32, PV>);
+                else launch(k_rotate<T, 48, PV>);
+            } else {
+                if (NO == 8) launch(k_rotate<T, 8, PV>);
+                else if (NO == 16) launch(k_rotate<T, 16, PV>);
+                else launch(k_rotate<T, 24, PV>);
+            }
         };
         profile_begin(st);
-        launch(k_rotate<T>);
+        if (vec && p == 1) pick(std::integral_constant<int, 1>());
+        else if (vec && p == 2) pick(std::integral_constant<int, 2>());
+        else if (vec && p == 4) pick(std::integral_constant<int, 4>());
+        else pick(std::integral_constant<int, 0>());  // scalar loads
         done("k_rotate", (double)op.D * Sproc * p * ((double)kc / p + (double)nout / p) * sizeof(T));
     }
     void gather_block(int Snew, int p, int ld_in, int ld_out, const int* in_idx, const T* Vin,
@@ -878,7 +1389,7 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
     DevBuf<T> Va((size_t)(nb + 1) * bmax), Vb((size_t)(nb + 1) * bmax), W((size_t)bmax);
     DevBuf<double> part((size_t)nch_max * kcap * S0 * p), gpart((size_t)nchu_max * p * S0 * p);
     DevBuf<T> Cf((size_t)kcap * S0 * p);
-    DevBuf<double> Rinv((size_t)S0 * p * p), Racc((size_t)S0 * p * p), Tm((size_t)S0 * Tdim * Tdim),
+    DevBuf<double> Rinv((size_t)3 * S0 * p * p), Racc((size_t)S0 * p * p), Tm((size_t)S0 * Tdim * Tdim),
         d_prm((size_t)3 * S0);
     DevBuf<unsigned char> dead((size_t)S0 * Tdim);
     DevBuf<int> d_in(S0), d_out(S0);
@@ -913,6 +1424,23 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
     auto orthonormalize = [&](const Geo& gu, int ncols, T* Wb, T* Vout, int jrow, bool gram_done) {
         T* scratch = Vb.p;
         double* Tj = jrow > 0 ? Tm.p : nullptr;
+        if (L.vec_ok(ncols, ncols, p, 0, Wb, Vout)) {
+            // factors in three slots; each pass re-reads W and applies them in registers
+            const int64_t rs = (int64_t)S * p * p;
+            if (!gram_done) L.normgram(gu, p, 0, Rinv.p, rs, Wb, nullptr, 1, gpart.p);
+            if (p == 1) {
+                L.qr(gu, S, p, gpart.p, 2, 0.0, Racc.p, Rinv.p, Tj, Tdim, jrow, kill_abs, dead.p);
+                L.normgram(gu, p, 1, Rinv.p, rs, Wb, Vout, 0, gpart.p);
+                return;
+            }
+            L.qr(gu, S, p, gpart.p, 0, shift_rel, Racc.p, Rinv.p, nullptr, Tdim, jrow, kill_abs, nullptr);
+            L.normgram(gu, p, 1, Rinv.p, rs, Wb, nullptr, 1, gpart.p);
+            L.qr(gu, S, p, gpart.p, 1, 0.0, Racc.p, Rinv.p + rs, nullptr, Tdim, jrow, kill_abs, nullptr);
+            L.normgram(gu, p, 2, Rinv.p, rs, Wb, nullptr, 1, gpart.p);
+            L.qr(gu, S, p, gpart.p, 2, 0.0, Racc.p, Rinv.p + 2 * rs, Tj, Tdim, jrow, kill_abs, dead.p);
+            L.normgram(gu, p, 3, Rinv.p, rs, Wb, Vout, 0, gpart.p);
+            return;
+        }
         if (!gram_done) L.update(gu, p, 0, 0, Va.p, Cf.p, Wb, 1, gpart.p);
         if (p == 1) {
             L.qr(gu, S, p, gpart.p, 2, 0.0, Racc.p, Rinv.p, Tj, Tdim, jrow, kill_abs, dead.p);
@@ -974,7 +1502,7 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
             L.dot(g, ncols, p, 1, bstride, Vj, W.p, kcap, part.p);
             L.local_coef(g, j, c_lo, p, kcap, part.p, Tm.p, Tdim, Cf.p);
             L.update(gu, p, (j + 1) * p - c_lo, bstride, Va.p + (int64_t)(c_lo / p) * bstride, Cf.p,
-                     W.p, 0, gpart.p);
+                     W.p, 0, gpart.p, "k_update(local)");
             // one full re-orthogonalisation pass, Gram matrix of the result
             const int kc = (j + 1) * p;
             L.dot(g, ncols, p, j + 1, bstride, Va.p, W.p, kcap, part.p);
