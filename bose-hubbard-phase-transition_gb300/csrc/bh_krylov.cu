@@ -810,15 +810,16 @@ k_normgram(int64_t D, int S, int nR, const double* __restrict__ Rinv, int64_t rs
 // ostride, row stride ld_out), or with single != 0 one row-major array
 // Vout[r][o nout + i].
 // A CTA takes Sg solves (their Y in shared memory, rows zero-padded to npad,
-// a multiple of NO, and solves ystride apart so that the Sg rows read together fall in different
-// banks) and a chunk of rows; thread = (solve ls = tid % Sg, row).  The Sg
-// solves of one row are adjacent in memory (one sector for Sg p = 32 B / T),
-// so a warp's loads cover whole sectors, and each Y row segment it reads is
-// shared by the 32 / Sg lanes of one solve (a broadcast).  NO outputs stay in
+// a multiple of NO, and solves ystride apart so that the Sg rows read together
+// fall in different banks) and a chunk of rows; thread = (solve ls = tid % Sg,
+// RB rows rstep apart).  The Sg solves of one row are adjacent in memory (one
+// sector for Sg p = 32 B / T), so a warp's loads cover whole sectors.  Each Y
+// value read from shared memory feeds RB rows' FMAs (shared memory, not the
+// FMA pipe, bounds a rotation with RB = 1).  NO outputs per row stay in
 // registers; more outputs take further passes over the inputs.  PV = p for
 // p in {1, 2, 4} (one vector load per basis block), else 0 (scalar loads).
-template <class T, int NO, int PV>
-__global__ void __launch_bounds__(256)
+template <class T, int NO, int PV, int RB>
+__global__ void __launch_bounds__(128)
 k_rotate(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t bstride,
          const T* __restrict__ V, const T* __restrict__ Yg, const int* __restrict__ in_idx,
          const int* __restrict__ out_idx, T* __restrict__ Vout, int64_t ostride, int ld_out,
@@ -842,19 +843,30 @@ k_rotate(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t bstri
     const int64_t r0 = (int64_t)blockIdx.y * rows_per_chunk;
     const int64_t r1 = min(D, r0 + rows_per_chunk);
     const T* ys = sY + (size_t)ls * ystride;
-    for (int64_t r = r0 + threadIdx.x / Sg; r < r1; r += rstep) {
-        const T* vr = V + r * ld_in + (int64_t)sin * p;
-        for (int o0 = 0; o0 < nout; o0 += NO) {
-            T acc[NO];
+    for (int64_t base = r0 + threadIdx.x / Sg; base < r1; base += (int64_t)RB * rstep) {
+        const T* vr[RB];
+        bool ok[RB];
 #pragma unroll
-            for (int u = 0; u < NO; ++u) acc[u] = T(0);
+        for (int k = 0; k < RB; ++k) {
+            const int64_t r = base + (int64_t)k * rstep;
+            ok[k] = r < r1;
+            vr[k] = V + (ok[k] ? r : base) * ld_in + (int64_t)sin * p;  // invalid rows read row base
+        }
+        for (int o0 = 0; o0 < nout; o0 += NO) {
+            T acc[RB][NO];
+#pragma unroll
+            for (int k = 0; k < RB; ++k)
+#pragma unroll
+                for (int u = 0; u < NO; ++u) acc[k][u] = T(0);
             if constexpr (PV >= 1) {
-                constexpr int UJ = PV == 1 ? 8 : (PV == 2 ? 4 : 2);
+                constexpr int UJ = PV == 1 ? 4 : 2;
                 for (int j = 0; j < nblk; j += UJ) {
-                    Vec<T, PV> x[UJ];
+                    Vec<T, PV> x[UJ][RB];
 #pragma unroll
                     for (int u = 0; u < UJ; ++u)
-                        if (j + u < nblk) x[u] = ldv<T, PV>(vr + (int64_t)(j + u) * bstride);
+#pragma unroll
+                        for (int k = 0; k < RB; ++k)
+                            if (j + u < nblk) x[u][k] = ldv<T, PV>(vr[k] + (int64_t)(j + u) * bstride);
 #pragma unroll
                     for (int u = 0; u < UJ; ++u) {
                         if (j + u < nblk) {
@@ -865,7 +877,9 @@ k_rotate(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t bstri
                                 for (int o = 0; o < NO; o += V4) {
                                     const Vec<T, V4> y = ldv<T, V4>(yc + o);
 #pragma unroll
-                                    for (int w = 0; w < V4; ++w) acc[o + w] += x[u].v[q] * y.v[w];
+                                    for (int k = 0; k < RB; ++k)
+#pragma unroll
+                                        for (int w = 0; w < V4; ++w) acc[k][o + w] += x[u][k].v[q] * y.v[w];
                                 }
                             }
                         }
@@ -873,28 +887,37 @@ k_rotate(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t bstri
                 }
             } else {
                 for (int c = 0; c < kc; ++c) {
-                    const T x = vr[(int64_t)(c / p) * bstride + c % p];
+                    T x[RB];
+#pragma unroll
+                    for (int k = 0; k < RB; ++k) x[k] = vr[k][(int64_t)(c / p) * bstride + c % p];
                     const T* yc = ys + (size_t)c * npad + o0;
 #pragma unroll
                     for (int o = 0; o < NO; o += V4) {
                         const Vec<T, V4> y = ldv<T, V4>(yc + o);
 #pragma unroll
-                        for (int w = 0; w < V4; ++w) acc[o + w] += x * y.v[w];
+                        for (int k = 0; k < RB; ++k)
+#pragma unroll
+                            for (int w = 0; w < V4; ++w) acc[k][o + w] += x[k] * y.v[w];
                     }
                 }
             }
             const int no = min(NO, nout - o0);
-            if (single) {
-                T* dst = Vout + r * ld_out + (int64_t)sout * nout + o0;
 #pragma unroll
-                for (int u = 0; u < NO; ++u)
-                    if (u < no) dst[u] = acc[u];
-            } else {
+            for (int k = 0; k < RB; ++k) {
+                if (!ok[k]) continue;
+                const int64_t r = base + (int64_t)k * rstep;
+                if (single) {
+                    T* dst = Vout + r * ld_out + (int64_t)sout * nout + o0;
 #pragma unroll
-                for (int u = 0; u < NO; ++u) {
-                    if (u < no) {
-                        const int i = o0 + u;
-                        Vout[(int64_t)(i / p) * ostride + r * ld_out + (int64_t)sout * p + i % p] = acc[u];
+                    for (int u = 0; u < NO; ++u)
+                        if (u < no) dst[u] = acc[k][u];
+                } else {
+#pragma unroll
+                    for (int u = 0; u < NO; ++u) {
+                        if (u < no) {
+                            const int i = o0 + u;
+                            Vout[(int64_t)(i / p) * ostride + r * ld_out + (int64_t)sout * p + i % p] = acc[k][u];
+                        }
                     }
                 }
             }
@@ -1219,7 +1242,7 @@ struct Launcher {
         kern<<<g.nchunks, g.NT, smem, st>>>(op.D, g.ncols, p, ilog2(p), kc, bstride, V, Cf, W,
                                             g.rows_per_chunk, do_gram, gpart);
         done(name ? name : (kc > 0 ? "k_update" : "k_update(gram)"),
-             (double)(kc > 0 ? kc + 2 : 1) * op.D * g.ncols * sizeof(T));
+             (double)(kc > 0 ? kc / p + 2 : 1) * op.D * g.ncols * sizeof(T));
     }
     template <int P>
     void updatev_t(const Geo& g, int kc, int64_t bstride, const T* V, const T* Cf, T* W, int do_gram,
@@ -1234,7 +1257,7 @@ struct Launcher {
         profile_begin(st);
         kern<<<g.nchunks, NT, smem, st>>>(op.D, S, kc / P, bstride, V, Cf, W, g.rows_per_chunk, do_gram, gpart);
         done(name ? name : (kc > 0 ? "k_update" : "k_update(gram)"),
-             (double)(kc > 0 ? kc + 2 : 1) * op.D * g.ncols * sizeof(T));
+             (double)(kc > 0 ? kc / P + 2 : 1) * op.D * g.ncols * sizeof(T));
     }
     void update(const Geo& g, int p, int kc, int64_t bstride, const T* V, const T* Cf, T* W,
                 int do_gram, double* gpart, const char* name = nullptr) const {
@@ -1290,8 +1313,7 @@ struct Launcher {
         constexpr int V4 = 16 / sizeof(T), E = 128 / sizeof(T);
         // outputs per pass (a template value below); Y rows padded to a whole
         // number of passes so that every pass reads inside its row
-        const int NO = sizeof(T) == 4 ? (nout <= 16 ? 16 : (nout <= 32 ? 32 : 48))
-                                      : (nout <= 8 ? 8 : (nout <= 16 ? 16 : 24));
+        const int NO = sizeof(T) == 4 ? (nout <= 16 ? 16 : 24) : (nout <= 8 ? 8 : 16);
         const int npad = (nout + NO - 1) / NO * NO;
         const int ystride = ((kc * npad + E - 1) / E) * E + V4;
         const size_t per = (size_t)ystride * sizeof(T);
@@ -1301,33 +1323,33 @@ struct Launcher {
         int Sg = std::max(1, std::min(8, (int)(32 / ((size_t)p * sizeof(T)))));
         Sg = std::min(Sg, std::max(1, (int)((size_t)smax / per)));
         Sg = std::min(Sg, Sproc);
-        while (Sg > 1 && 256 % Sg != 0) --Sg;
+        while (Sg > 1 && 128 % Sg != 0) --Sg;
         const size_t smem = (size_t)Sg * per;
         const int ngroups = (Sproc + Sg - 1) / Sg;
-        const int rstep = 256 / Sg;
+        const int rstep = 128 / Sg;
         int64_t chunks = std::max<int64_t>(1, (6LL * sm_count() + ngroups - 1) / ngroups);
         int64_t rpc = (op.D + chunks - 1) / chunks;
-        rpc = std::max<int64_t>(rpc, rstep);
+        rpc = std::max<int64_t>(rpc, 4LL * rstep);
         chunks = (op.D + rpc - 1) / rpc;
         BH_REQUIRE(chunks <= 65535, "too many row chunks for the rotation grid");
         const bool vec = (p == 1 || p == 2 || p == 4) && ld_in % p == 0 && bstride % p == 0 &&
                          ((uintptr_t)V % ((uintptr_t)p * sizeof(T))) == 0;
         auto launch = [&](auto kern) {
             if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            kern<<<dim3((unsigned)ngroups, (unsigned)chunks), 256, smem, st>>>(
+            kern<<<dim3((unsigned)ngroups, (unsigned)chunks), 128, smem, st>>>(
                 op.D, Sproc, ld_in, p, kc, nout, bstride, V, Yg, in_idx, out_idx, Vout, ostride,
                 ld_out, single, Sg, npad, ystride, rpc);
         };
         auto pick = [&](auto pv) {
             constexpr int PV = decltype(pv)::value;
+            // RB rows per thread: 4 on the FP32 vector path, else 1
+            constexpr int RB = (sizeof(T) == 4 && PV >= 1) ? 4 : 1;
             if constexpr (sizeof(T) == 4) {
-                if (NO == 16) launch(k_rotate<T, 16, PV>);
-                else if (NO == 32) launch(k_rotate<T, 32, PV>);
-                else launch(k_rotate<T, 48, PV>);
+                if (NO == 16) launch(k_rotate<T, 16, PV, RB>);
+                else launch(k_rotate<T, 24, PV, RB>);
             } else {
-                if (NO == 8) launch(k_rotate<T, 8, PV>);
-                else if (NO == 16) launch(k_rotate<T, 16, PV>);
-                else launch(k_rotate<T, 24, PV>);
+                if (NO == 8) launch(k_rotate<T, 8, PV, RB>);
+                else launch(k_rotate<T, 16, PV, RB>);
             }
         };
         profile_begin(st);
