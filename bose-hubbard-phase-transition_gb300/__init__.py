@@ -54,6 +54,7 @@ EXPORTS = [
     "bh_last_error", "bh_version", "bh_neighbours_chain", "bh_neighbours_square",
     "bh_neighbours_cube", "bh_dimension", "bh_basis_create", "bh_basis_destroy",
     "bh_basis_info", "bh_basis_copy", "bh_basis_index", "bh_hamiltonian_create",
+    "bh_hamiltonian_create_matrix_free", "bh_hamiltonian_is_matrix_free",
     "bh_hamiltonian_destroy", "bh_hamiltonian_nnz", "bh_hamiltonian_csr",
     "bh_hamiltonian_apply", "bh_hamiltonian_apply_noalloc", "bh_solver_opts_default", "bh_eigsh", "bh_eigsh_csr",
     "bh_eigsh_batch", "bh_dense_eigh", "bh_gap_ratios", "bh_spdm", "bh_phase_map", "bh_profile_enable",
@@ -86,6 +87,8 @@ def load() -> C.CDLL:
     L.bh_basis_copy.argtypes = [vp, vp, vp, vp, vp]
     L.bh_basis_index.argtypes = [vp, C.c_int64, vp, vp]
     L.bh_hamiltonian_create.argtypes = [vp, vp, vp, C.POINTER(vp)]
+    L.bh_hamiltonian_create_matrix_free.argtypes = [vp, vp, vp, C.POINTER(vp)]
+    L.bh_hamiltonian_is_matrix_free.argtypes = [vp, C.POINTER(C.c_int)]
     L.bh_hamiltonian_destroy.argtypes = [vp]
     L.bh_hamiltonian_nnz.argtypes = [vp, i64p]
     L.bh_hamiltonian_csr.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, vp, vp, vp]
@@ -224,15 +227,21 @@ class SolveInfo:
 
 
 class Hamiltonian:
-    """H = J T + U V - mu N of one sector, assembled on the device once."""
+    """H = J T + U V - mu N of one sector, assembled on the device once.
 
-    def __init__(self, basis: Basis, neighbours):
+    matrix_free=True keeps no matrix entries: each product regenerates the
+    rows from packed occupation strings (bh_hamiltonian_create_matrix_free).
+    """
+
+    def __init__(self, basis: Basis, neighbours, matrix_free: bool = False):
         self.basis = basis
         off, flat = flatten_neighbours(neighbours)
         if len(off) != basis.m + 1:
             raise ValueError("neighbour lists must have one entry per site")
         self._h = C.c_void_p()
-        _check(load().bh_hamiltonian_create(basis._h, _ptr(off), _ptr(flat), C.byref(self._h)))
+        create = load().bh_hamiltonian_create_matrix_free if matrix_free else load().bh_hamiltonian_create
+        _check(create(basis._h, _ptr(off), _ptr(flat), C.byref(self._h)))
+        self.matrix_free = bool(matrix_free)
         nnz = C.c_int64()
         _check(load().bh_hamiltonian_nnz(self._h, C.byref(nnz)))
         self.nnz_offdiag = nnz.value

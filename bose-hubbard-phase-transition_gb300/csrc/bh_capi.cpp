@@ -202,36 +202,42 @@ int bh_basis_index(const bh_basis* b, int64_t nq, const uint8_t* occ, int32_t* c
 }
 
 // ---- Hamiltonian ----
+static bh_hamiltonian* new_hamiltonian(const bh_basis* b, const int32_t* nbr_off, const int32_t* nbr) {
+    BH_REQUIRE(b != nullptr && nbr_off != nullptr, "null argument");
+    const int m = b->m;
+    BH_REQUIRE(nbr_off[0] == 0, "neighbour offsets must start at 0");
+    for (int i = 0; i < m; ++i) BH_REQUIRE(nbr_off[i + 1] >= nbr_off[i], "neighbour offsets must be non-decreasing");
+    const int tot = nbr_off[m];
+    BH_REQUIRE(tot == 0 || nbr != nullptr, "neighbour list is null");
+    std::vector<int> cnt((size_t)m * m, 0);
+    for (int i = 0; i < m; ++i)
+        for (int k = nbr_off[i]; k < nbr_off[i + 1]; ++k) {
+            const int j = nbr[k];
+            BH_REQUIRE(j >= 0 && j < m, "neighbour index out of range");
+            BH_REQUIRE(j != i, "self-bond in the neighbour list");
+            cnt[(size_t)i * m + j] += 1;
+        }
+    for (int i = 0; i < m; ++i)
+        for (int j = 0; j < m; ++j)
+            BH_REQUIRE(cnt[(size_t)i * m + j] == cnt[(size_t)j * m + i], "neighbour lists must be symmetric");
+    auto* h = new bh_hamiltonian();
+    h->basis = b;
+    h->m = m;
+    h->n = b->n;
+    h->D = b->D;
+    h->device = b->device;
+    h->h_nbr_off.assign(nbr_off, nbr_off + m + 1);
+    h->h_nbr.assign(nbr, nbr + tot);
+    return h;
+}
+
 int bh_hamiltonian_create(const bh_basis* b, const int32_t* nbr_off, const int32_t* nbr,
                           bh_hamiltonian** out) {
     return guard([&] {
-        BH_REQUIRE(b != nullptr && nbr_off != nullptr && out != nullptr, "null argument");
+        BH_REQUIRE(out != nullptr, "null argument");
         *out = nullptr;
-        const int m = b->m;
-        BH_REQUIRE(nbr_off[0] == 0, "neighbour offsets must start at 0");
-        for (int i = 0; i < m; ++i) BH_REQUIRE(nbr_off[i + 1] >= nbr_off[i], "neighbour offsets must be non-decreasing");
-        const int tot = nbr_off[m];
-        BH_REQUIRE(tot == 0 || nbr != nullptr, "neighbour list is null");
-        std::vector<int> cnt((size_t)m * m, 0);
-        for (int i = 0; i < m; ++i)
-            for (int k = nbr_off[i]; k < nbr_off[i + 1]; ++k) {
-                const int j = nbr[k];
-                BH_REQUIRE(j >= 0 && j < m, "neighbour index out of range");
-                BH_REQUIRE(j != i, "self-bond in the neighbour list");
-                cnt[(size_t)i * m + j] += 1;
-            }
-        for (int i = 0; i < m; ++i)
-            for (int j = 0; j < m; ++j)
-                BH_REQUIRE(cnt[(size_t)i * m + j] == cnt[(size_t)j * m + i], "neighbour lists must be symmetric");
-        auto* h = new bh_hamiltonian();
+        bh_hamiltonian* h = new_hamiltonian(b, nbr_off, nbr);
         try {
-            h->basis = b;
-            h->m = m;
-            h->n = b->n;
-            h->D = b->D;
-            h->device = b->device;
-            h->h_nbr_off.assign(nbr_off, nbr_off + m + 1);
-            h->h_nbr.assign(nbr, nbr + tot);
             Stream st;
             hamiltonian_build(h, st);
         } catch (...) {
@@ -239,6 +245,30 @@ int bh_hamiltonian_create(const bh_basis* b, const int32_t* nbr_off, const int32
             throw;
         }
         *out = h;
+    });
+}
+
+int bh_hamiltonian_create_matrix_free(const bh_basis* b, const int32_t* nbr_off, const int32_t* nbr,
+                                      bh_hamiltonian** out) {
+    return guard([&] {
+        BH_REQUIRE(out != nullptr, "null argument");
+        *out = nullptr;
+        bh_hamiltonian* h = new_hamiltonian(b, nbr_off, nbr);
+        try {
+            Stream st;
+            hamiltonian_build_matrix_free(h, st);
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
+int bh_hamiltonian_is_matrix_free(const bh_hamiltonian* h, int* matrix_free) {
+    return guard([&] {
+        BH_REQUIRE(h != nullptr && matrix_free != nullptr, "null argument");
+        *matrix_free = h->matrix_free ? 1 : 0;
     });
 }
 
@@ -270,26 +300,8 @@ int bh_hamiltonian_csr(const bh_hamiltonian* h, int order, double J, double U, d
     });
 }
 
-static OpView<double> op64_of(const bh_hamiltonian* h) {
-    OpView<double> o;
-    o.rp = h->d_rp.p;
-    o.ci = h->d_ci.p;
-    o.tv = h->d_tv64.p;
-    o.vd = h->d_vd64.p;
-    o.D = h->D;
-    o.rp_nnz = h->nnz;
-    return o;
-}
-static OpView<float> op32_of(const bh_hamiltonian* h) {
-    OpView<float> o;
-    o.rp = h->d_rp.p;
-    o.ci = h->d_ci.p;
-    o.tv = h->d_tv32.p;
-    o.vd = h->d_vd32.p;
-    o.D = h->D;
-    o.rp_nnz = h->nnz;
-    return o;
-}
+static OpView<double> op64_of(const bh_hamiltonian* h) { return op_view<double>(h); }
+static OpView<float> op32_of(const bh_hamiltonian* h) { return op_view<float>(h); }
 
 int bh_hamiltonian_apply(const bh_hamiltonian* h, int order, double J, double U, double mu,
                          int nvec, const double* x, double* y) {

@@ -342,6 +342,83 @@ void hamiltonian_build(bh_hamiltonian* h, cudaStream_t st) {
     BH_CUDA(cudaStreamSynchronize(st));
 }
 
+int occupation_bits(int m, int n) {
+    int b = 1;
+    while ((1 << b) - 1 < n) ++b;
+    return (int64_t)m * b <= 64 ? b : 0;
+}
+
+// Packed occupation string of each lexicographic state: site i in bits
+// [bits i, bits (i + 1)).
+__global__ void k_pack_occ(uint32_t D, int m, int n, int bits, const uint32_t* __restrict__ rt,
+                           uint64_t* __restrict__ out) {
+    extern __shared__ uint32_t s_rt[];
+    const int nrt = (m > 1 ? m - 1 : 1) * (n + 1);
+    for (int i = threadIdx.x; i < nrt; i += blockDim.x) s_rt[i] = rt[i];
+    __syncthreads();
+    uint8_t occ[kMaxSites];
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < D; r += gridDim.x * blockDim.x) {
+        unrank_state(r, m, n, s_rt, occ);
+        uint64_t w = 0;
+        for (int i = 0; i < m; ++i) w |= (uint64_t)occ[i] << (bits * i);
+        out[r] = w;
+    }
+}
+
+void hamiltonian_build_matrix_free(bh_hamiltonian* h, cudaStream_t st) {
+    const bh_basis* b = h->basis;
+    const int bits = occupation_bits(h->m, h->n);
+    BH_REQUIRE(bits > 0, "matrix-free operator: the occupations of m sites do not fit 64 bits");
+    std::vector<int32_t> hbi, hbj;
+    bond_arrays(h, hbi, hbj);
+    const int nb = (int)hbi.size();
+    BH_REQUIRE(nb <= 128, "matrix-free operator: at most 128 directed bonds");
+    h->matrix_free = true;
+    h->occ_bits = bits;
+    h->nbonds = nb;
+    std::vector<uint8_t> hb((size_t)2 * nb);
+    for (int k = 0; k < nb; ++k) {
+        hb[2 * k] = (uint8_t)hbi[k];
+        hb[2 * k + 1] = (uint8_t)hbj[k];
+    }
+    h->d_bonds.alloc(hb.size());
+    if (nb) BH_CUDA(cudaMemcpyAsync(h->d_bonds.p, hb.data(), hb.size(), cudaMemcpyHostToDevice, st));
+    // hop amplitudes -sqrt(n_i (n_j + 1)) by table, a = n_i (n_j + 1) <= n (n + 1)
+    const int na = h->n * (h->n + 1) + 1;
+    std::vector<double> sq64(na);
+    std::vector<float> sq32(na);
+    for (int a = 0; a < na; ++a) {
+        sq64[a] = -std::sqrt((double)a);
+        sq32[a] = (float)sq64[a];
+    }
+    h->d_sq64.alloc(na);
+    h->d_sq32.alloc(na);
+    BH_CUDA(cudaMemcpyAsync(h->d_sq64.p, sq64.data(), na * sizeof(double), cudaMemcpyHostToDevice, st));
+    BH_CUDA(cudaMemcpyAsync(h->d_sq32.p, sq32.data(), na * sizeof(float), cudaMemcpyHostToDevice, st));
+    h->d_occ.alloc(h->D);
+    const size_t smem = b->rt.host.size() * sizeof(uint32_t);
+    int64_t g = (h->D + 255) / 256;
+    if (g > sm_count() * 16) g = sm_count() * 16;
+    k_pack_occ<<<(unsigned)(g < 1 ? 1 : g), 256, smem, st>>>((uint32_t)h->D, h->m, h->n, bits,
+                                                             b->d_rt.p, h->d_occ.p);
+    BH_CUDA(cudaGetLastError());
+    // entries of the equivalent stored T (duplicate bonds merged), for reporting
+    DevBuf<int64_t> counts(h->D + 1), rp(h->D + 1);
+    DevBuf<int32_t> dbi(nb), dbj(nb);
+    if (nb) {
+        BH_CUDA(cudaMemcpyAsync(dbi.p, hbi.data(), nb * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+        BH_CUDA(cudaMemcpyAsync(dbj.p, hbj.data(), nb * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    }
+    BH_CUDA(cudaMemsetAsync(counts.p, 0, (h->D + 1) * sizeof(int64_t), st));
+    k_csr_rows<false><<<warp_grid(h->D), 256, smem, st>>>((uint32_t)h->D, h->m, h->n, b->d_rt.p, dbi.p,
+                                                          dbj.p, nb, nullptr, nullptr, 0, 1.0, 0.0, 0.0,
+                                                          counts.p, nullptr, nullptr, nullptr, nullptr);
+    BH_CUDA(cudaGetLastError());
+    scan_exclusive_i64(counts.p, rp.p, h->D + 1, st);
+    BH_CUDA(cudaMemcpyAsync(&h->nnz, rp.p + h->D, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    BH_CUDA(cudaStreamSynchronize(st));
+}
+
 void hamiltonian_csr(const bh_hamiltonian* h, int order, double J, double U, double mu,
                      int64_t* d_rp, int32_t* d_ci, double* d_val, cudaStream_t st) {
     const bh_basis* b = h->basis;

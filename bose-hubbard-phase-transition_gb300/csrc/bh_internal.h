@@ -125,6 +125,15 @@ struct bh_hamiltonian {
     // diagonal V in lexicographic order
     bh::DevBuf<double> d_vd64;
     bh::DevBuf<float> d_vd32;
+    // matrix-free variant: no stored T or V; packed occupation strings (lex
+    // order), the directed bonds and the table of -sqrt(a) instead
+    bool matrix_free = false;
+    int occ_bits = 0;
+    int nbonds = 0;
+    bh::DevBuf<uint64_t> d_occ;
+    bh::DevBuf<uint8_t> d_bonds;
+    bh::DevBuf<double> d_sq64;
+    bh::DevBuf<float> d_sq32;
 };
 
 namespace bh {
@@ -138,6 +147,10 @@ void scan_exclusive_i64(const int64_t* d_in, int64_t* d_out, int64_t n, cudaStre
 
 // ---- launchers (bh_hamiltonian.cu) ----
 void hamiltonian_build(bh_hamiltonian* h, cudaStream_t st);
+// matrix-free variant: packed occupations, bonds, -sqrt table and the entry count
+void hamiltonian_build_matrix_free(bh_hamiltonian* h, cudaStream_t st);
+// bits per site of the packed occupation strings (0 if m sites do not fit 64 bits)
+int occupation_bits(int m, int n);
 // CSR of H = J T + U V - mu N with diagonal entries, rows/cols in `order`.
 void hamiltonian_csr(const bh_hamiltonian* h, int order, double J, double U, double mu,
                      int64_t* d_rp, int32_t* d_ci, double* d_val, cudaStream_t st);

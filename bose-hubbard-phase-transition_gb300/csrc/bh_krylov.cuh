@@ -15,7 +15,44 @@ struct OpView {
     const T* vd = nullptr;
     int64_t D = 0;
     int64_t rp_nnz = 0;  // stored entries (for the algorithmic byte count)
+    // matrix-free operator (occ != nullptr): the rows of T and V are
+    // regenerated in every product from the packed occupation strings
+    const uint64_t* occ = nullptr;   // D strings, `bits` bits per site, site 0 in the low bits
+    const uint32_t* rt = nullptr;    // rank table (m-1) x (n+1)
+    const uint8_t* bonds = nullptr;  // directed bonds: bonds[2k] = i, bonds[2k+1] = j
+    const T* sq = nullptr;           // sq[a] = -sqrt(a), a <= n (n + 1)
+    int m = 0, n = 0, bits = 0, nbonds = 0;
 };
+
+// Operator views of a built Hamiltonian (CSR or matrix-free).
+template <class T>
+inline OpView<T> op_view(const bh_hamiltonian* h) {
+    OpView<T> o;
+    o.D = h->D;
+    o.rp_nnz = h->nnz;
+    if (h->matrix_free) {
+        o.occ = h->d_occ.p;
+        o.rt = h->basis->d_rt.p;
+        o.bonds = h->d_bonds.p;
+        if constexpr (sizeof(T) == 8) o.sq = reinterpret_cast<const T*>(h->d_sq64.p);
+        else o.sq = reinterpret_cast<const T*>(h->d_sq32.p);
+        o.m = h->m;
+        o.n = h->n;
+        o.bits = h->occ_bits;
+        o.nbonds = h->nbonds;
+        return o;
+    }
+    o.rp = h->d_rp.p;
+    o.ci = h->d_ci.p;
+    if constexpr (sizeof(T) == 8) {
+        o.tv = reinterpret_cast<const T*>(h->d_tv64.p);
+        o.vd = reinterpret_cast<const T*>(h->d_vd64.p);
+    } else {
+        o.tv = reinterpret_cast<const T*>(h->d_tv32.p);
+        o.vd = reinterpret_cast<const T*>(h->d_vd32.p);
+    }
+    return o;
+}
 
 struct SolveRequest {
     int S = 1;                 // solves in the batch (share the operator pattern)

@@ -81,13 +81,7 @@ extern "C" int bh_hamiltonian_apply_noalloc(const bh_hamiltonian* h, int order, 
         BH_REQUIRE(dev == h->device, "the current device is not the Hamiltonian's device");
         double* s = bh::apply_scratch_address();
         cudaStream_t st = static_cast<cudaStream_t>(stream);
-        bh::OpView<double> op;
-        op.rp = h->d_rp.p;
-        op.ci = h->d_ci.p;
-        op.tv = h->d_tv64.p;
-        op.vd = h->d_vd64.p;
-        op.D = D;
-        op.rp_nnz = h->nnz;
+        const bh::OpView<double> op = bh::op_view<double>(h);
         double* prm = s;
         bh::k_set_params<<<1, 32, 0, st>>>(prm, J, U, -mu * (double)h->n);
         BH_CUDA(cudaGetLastError());

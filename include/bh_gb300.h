@@ -106,8 +106,21 @@ int bh_basis_index(const bh_basis* b, int64_t nq, const uint8_t* occ, int32_t* c
  * must be symmetric and free of self-bonds. */
 int bh_hamiltonian_create(const bh_basis* b, const int32_t* nbr_off, const int32_t* nbr,
                           bh_hamiltonian** out);
+/* The same operator without stored matrix entries (replaces the same
+ * reference functions as bh_hamiltonian_create): every product regenerates
+ * the rows of T and V from the states' occupations packed into one uint64
+ * each (ceil(log2(n+1)) bits per site, so m * bits <= 64 is required), with
+ * combinadic ranking of each hopped state; at most 128 directed bonds.
+ * Device memory: 8 bytes per state instead of about 12 per stored entry.
+ * Every entry point that takes a Hamiltonian accepts either kind;
+ * bh_hamiltonian_csr assembles the stored form on request. */
+int bh_hamiltonian_create_matrix_free(const bh_basis* b, const int32_t* nbr_off,
+                                      const int32_t* nbr, bh_hamiltonian** out);
+/* *matrix_free = 1 for a Hamiltonian made by bh_hamiltonian_create_matrix_free. */
+int bh_hamiltonian_is_matrix_free(const bh_hamiltonian* h, int* matrix_free);
 int bh_hamiltonian_destroy(bh_hamiltonian* h);
-/* Number of stored off-diagonal entries of T. */
+/* Number of off-diagonal entries of T (stored, or of the equivalent stored
+ * form for a matrix-free Hamiltonian). */
 int bh_hamiltonian_nnz(const bh_hamiltonian* h, int64_t* nnz_offdiag);
 /* Writes H = J T + U V - mu N as CSR into host buffers, rows and columns in
  * `order`, with one (explicit, possibly zero) diagonal entry per row and
