@@ -57,7 +57,7 @@ EXPORTS = [
     "bh_hamiltonian_create_matrix_free", "bh_hamiltonian_is_matrix_free",
     "bh_hamiltonian_destroy", "bh_hamiltonian_nnz", "bh_hamiltonian_csr",
     "bh_hamiltonian_apply", "bh_hamiltonian_apply_noalloc", "bh_solver_opts_default", "bh_eigsh", "bh_eigsh_csr",
-    "bh_eigsh_batch", "bh_dense_eigh", "bh_gap_ratios", "bh_spdm", "bh_phase_map", "bh_profile_enable",
+    "bh_eigsh_batch", "bh_dense_eigh", "bh_gap_ratios", "bh_spdm", "bh_phase_map", "bh_scmf", "bh_mean_field_grid", "bh_profile_enable",
     "bh_profile_reset", "bh_profile_count", "bh_profile_get",
 ]
 
@@ -107,6 +107,9 @@ def load() -> C.CDLL:
     L.bh_gap_ratios.argtypes = [C.c_int, vp, vp, f64p]
     L.bh_spdm.argtypes = [vp, C.c_int, vp, vp]
     L.bh_phase_map.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, vp, C.c_int, vp, vp, vp]
+    L.bh_scmf.argtypes = [C.c_int, vp, vp, C.c_int, vp, C.c_int, vp, vp]
+    L.bh_mean_field_grid.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(C.c_int),
+                                     C.POINTER(C.c_int), vp, vp, vp]
     L.bh_profile_enable.argtypes = [C.c_int]
     L.bh_profile_count.argtypes = [C.POINTER(C.c_int)]
     L.bh_profile_get.argtypes = [C.c_int, C.c_char_p, C.c_int, i64p, f64p, f64p]
@@ -456,3 +459,39 @@ class Analysis:
         _check(load().bh_phase_map(m, n_lo, nsec, nJ, _ptr(e0), len(mu), _ptr(mu), _ptr(dens),
                                    _ptr(kap)))
         return dens, kap
+
+    # ---- mean field (analysis.cpp:58-178) ----
+    @staticmethod
+    def SCMF(mu, J, q: int, psi0, precision: int):
+        """Self-consistent mean-field order parameter for each (mu, J, psi0)
+        point (arrays broadcast together); returns (psi, iterations)."""
+        mu, J, psi0 = np.broadcast_arrays(np.asarray(mu, np.float64), np.asarray(J, np.float64),
+                                          np.asarray(psi0, np.float64))
+        shape = mu.shape
+        mu, J, psi0 = (np.ascontiguousarray(a.ravel()) for a in (mu, J, psi0))
+        psi = np.zeros(mu.size)
+        it = np.zeros(mu.size, np.int32)
+        _check(load().bh_scmf(mu.size, _ptr(mu), _ptr(J), q, _ptr(psi0), precision, _ptr(psi),
+                              _ptr(it)))
+        return psi.reshape(shape), it.reshape(shape)
+
+    @staticmethod
+    def mean_field_parameters(n: int, precision: int, q: int = 1, seed: int = 0,
+                              path: str | None = None):
+        """The reference's mean-field sweep (mu in [0, 4), J in [0, 0.25), n
+        steps each): returns (mu, J, psi[len(mu), len(J)]) and, with path,
+        writes the reference's "mu J psi" lines (mean_field.txt)."""
+        mu = np.zeros(n + 1)
+        J = np.zeros(n + 1)
+        psi = np.zeros((n + 1) * (n + 1))
+        a, b = C.c_int(), C.c_int()
+        _check(load().bh_mean_field_grid(n, precision, q, seed, C.byref(a), C.byref(b), _ptr(mu),
+                                         _ptr(J), _ptr(psi)))
+        mu, J = mu[: a.value], J[: b.value]
+        psi = psi[: a.value * b.value].reshape(a.value, b.value)
+        if path:
+            with open(path, "w") as f:
+                for i, x in enumerate(mu):
+                    for k, y in enumerate(J):
+                        f.write(f"{x:g} {y:g} {psi[i, k]:g}\n")
+        return mu, J, psi

@@ -513,3 +513,65 @@ int bh_phase_map(int m, int n_lo, int nsec, int nJ, const double* e0, int nmu, c
 }
 
 }  // extern "C"
+
+// ---- mean field ----
+int bh_scmf(int npts, const double* mu, const double* J, int q, const double* psi0, int precision,
+            double* psi, int* iters) {
+    return guard([&] {
+        BH_REQUIRE(npts >= 0, "npts must be >= 0");
+        BH_REQUIRE(npts == 0 || (mu && J && psi0 && psi), "null argument");
+        BH_REQUIRE(q >= 0 && precision >= 0 && precision <= 15, "q must be >= 0 and precision in [0, 15]");
+        if (npts == 0) return;
+        Stream st;
+        DevBuf<double> dm(npts), dj(npts), dp0(npts), dp(npts);
+        DevBuf<int> di(npts);
+        BH_CUDA(cudaMemcpyAsync(dm.p, mu, npts * sizeof(double), cudaMemcpyHostToDevice, st));
+        BH_CUDA(cudaMemcpyAsync(dj.p, J, npts * sizeof(double), cudaMemcpyHostToDevice, st));
+        BH_CUDA(cudaMemcpyAsync(dp0.p, psi0, npts * sizeof(double), cudaMemcpyHostToDevice, st));
+        scmf_device(npts, dm.p, dj.p, q, dp0.p, precision, 20000, dp.p, di.p, st);
+        BH_CUDA(cudaMemcpyAsync(psi, dp.p, npts * sizeof(double), cudaMemcpyDeviceToHost, st));
+        std::vector<int> hi(npts);
+        BH_CUDA(cudaMemcpyAsync(hi.data(), di.p, npts * sizeof(int), cudaMemcpyDeviceToHost, st));
+        BH_CUDA(cudaStreamSynchronize(st));
+        if (iters) std::memcpy(iters, hi.data(), npts * sizeof(int));
+    });
+}
+
+// uniform [0, 1) from splitmix64 of (seed, k)
+static double mf_seed_value(uint64_t seed, uint64_t k) {
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (k + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+int bh_mean_field_grid(int n, int precision, int q, uint64_t seed, int* nmu, int* nJ,
+                       double* mu_out, double* J_out, double* psi_out) {
+    return guard([&] {
+        BH_REQUIRE(n >= 1 && nmu && nJ && mu_out && J_out && psi_out, "null argument or n < 1");
+        // the reference's loops: x = x_min, x += dx while x < x_max (analysis.cpp:60-79)
+        const double J_min = 0.0, J_max = 0.25, mu_min = 0.0, mu_max = 4.0;
+        const double dJ = (J_max - J_min) / n, dmu = (mu_max - mu_min) / n;
+        std::vector<double> mus, Js;
+        for (double x = mu_min; x < mu_max; x += dmu) mus.push_back(x);
+        for (double x = J_min; x < J_max; x += dJ) Js.push_back(x);
+        BH_REQUIRE((int)mus.size() <= n + 1 && (int)Js.size() <= n + 1, "grid longer than n + 1");
+        const int a = (int)mus.size(), b = (int)Js.size();
+        std::vector<double> pm((size_t)a * b), pj((size_t)a * b), p0((size_t)a * b);
+        for (int i = 0; i < a; ++i)
+            for (int k = 0; k < b; ++k) {
+                const size_t idx = (size_t)i * b + k;
+                pm[idx] = mus[i];
+                pj[idx] = Js[k];
+                p0[idx] = mf_seed_value(seed, idx);
+            }
+        std::vector<int> it((size_t)a * b);
+        const int rc = bh_scmf(a * b, pm.data(), pj.data(), q, p0.data(), precision, psi_out, it.data());
+        if (rc != BH_OK) throw Error(rc, bh_last_error());
+        std::memcpy(mu_out, mus.data(), a * sizeof(double));
+        std::memcpy(J_out, Js.data(), b * sizeof(double));
+        *nmu = a;
+        *nJ = b;
+    });
+}

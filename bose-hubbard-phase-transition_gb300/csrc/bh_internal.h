@@ -163,6 +163,12 @@ void gather_rows(int64_t D, int ncols, const int32_t* d_map, const double* d_in,
 void phase_map_device(int m, int n_lo, int nsec, int nJ, const double* d_e0, int nmu,
                       const double* d_mu, double* d_density, double* d_kappa, cudaStream_t st);
 
+// ---- mean field (bh_meanfield.cu) ----
+// psi[k] of the self-consistent mean-field iteration at (mu[k], J[k]) from
+// psi0[k]; iters[k] = outer iterations (-1: truncation limit, -2: max_outer)
+void scmf_device(int npts, const double* d_mu, const double* d_J, int q, const double* d_psi0,
+                 int precision, int max_outer, double* d_psi, int* d_iters, cudaStream_t st);
+
 // ---- lattices (bh_lattice.cpp) ----
 using Lists = std::vector<std::vector<int32_t>>;
 Lists chain_lists(int m, bool closed);

@@ -225,6 +225,31 @@ int bh_phase_map(int m, int n_lo, int nsec, int nJ, const double* e0, int nmu, c
                  double* density, double* compressibility);
 
 /* ---------------------------------------------------------------------- */
+/* Mean field                                                              */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces Analysis::SCMF / SF_density (analysis.cpp:93-178) with BH::h_MF
+ * (hamiltonian.cpp:290-309) for npts points at once, one device thread per
+ * point: psi[k] is the self-consistent order parameter at (mu[k], J[k]) with
+ * q neighbours from the seed psi0[k], to eps = 10^-precision (precision in
+ * [0, 15]).  iters[k] (optional) = psi updates, -1 where the truncation would
+ * exceed 2p+1 = 97 levels (psi NaN), -2 where psi still moved after 20000
+ * updates.  Where psi = 0 or J = 0 the single-site matrix is diagonal and its
+ * ground vector is the first lowest level, so psi = 0 stays 0 (the
+ * reference's Lanczos mixes tied levels there, at integer mu). */
+int bh_scmf(int npts, const double* mu, const double* J, int q, const double* psi0, int precision,
+            double* psi, int* iters);
+/* Replaces Analysis::mean_field_parameters (analysis.cpp:58-89): the grid
+ * mu = 0, dmu, ... < 4 and J = 0, dJ, ... < 0.25 (dmu = 4/n, dJ = 0.25/n,
+ * built by repeated addition as the reference's range loops are, so up to
+ * n + 1 values each), seeds psi0 uniform in [0, 1) from splitmix64(seed, k)
+ * (the reference draws them from std::random_device).  mu_out and J_out need
+ * n + 1 entries, psi_out (n + 1)^2; on return psi_out[i * nJ + k] belongs to
+ * (mu_out[i], J_out[k]). */
+int bh_mean_field_grid(int n, int precision, int q, uint64_t seed, int* nmu, int* nJ,
+                       double* mu_out, double* J_out, double* psi_out);
+
+/* ---------------------------------------------------------------------- */
 /* Tracing (no counterpart in the reference beyond Resource::timer,        */
 /* src/resource.cpp:55-71): per-kernel device time from CUDA events.       */
 /* ---------------------------------------------------------------------- */

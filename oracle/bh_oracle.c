@@ -36,6 +36,11 @@
  *   - Analysis::coherence                     src/analysis.cpp:542-556
  *   - single-particle density matrix <phi|b+_i b_j|phi> (the quantity that
  *     Analysis::SPDM / braket, src/analysis.cpp:497-528 and 562-594, intend).
+ *   - the self-consistent mean-field order parameter: BH::h_MF
+ *     (src/hamiltonian.cpp:290-309), Analysis::SF_density and Analysis::SCMF
+ *     (src/analysis.cpp:93-178), with the smallest eigenpair of each
+ *     (2p+1) x (2p+1) matrix from a dense symmetric eigensolve (the reference
+ *     asks Spectra's SymEigsSolver for the same pair).
  *
  * Floating-point note: the tag sum is evaluated without contraction
  * (compile with -ffp-contract=off) so that it is the plain multiply-then-add
@@ -830,4 +835,81 @@ double bho_condensate_fraction(int m, const double* rho) {
     free(a);
     free(w);
     return fabs(mx / tr);
+}
+
+/* ------------------------------------------------------------------ */
+/* self-consistent mean field (src/analysis.cpp:93-178)               */
+/* ------------------------------------------------------------------ */
+
+/* Smallest eigenpair of the (2p+1) x (2p+1) matrix of BH::h_MF
+ * (src/hamiltonian.cpp:290-309): diagonal -mu i + i (i-1) / 2 + q J psi^2,
+ * entries (i+1, i) = (i, i+1) = -q J psi sqrt(i+1).  phi gets the vector. */
+static int scmf_ground(double psi, int p, double mu, double J, int q, double* phi, double* e0) {
+    const int N = 2 * p + 1;
+    double* a = (double*)calloc((size_t)N * N, sizeof(double));
+    double* w = (double*)malloc(sizeof(double) * N);
+    if (!a || !w) {
+        free(a);
+        free(w);
+        return 1;
+    }
+    for (int i = 0; i < N; ++i) a[(size_t)i * N + i] = -mu * i + 0.5 * i * (i - 1) + q * J * psi * psi;
+    for (int i = 0; i + 1 < N; ++i) {
+        const double v = -q * J * psi * sqrt((double)(i + 1));
+        a[(size_t)i * N + i + 1] = v;
+        a[(size_t)(i + 1) * N + i] = v;
+    }
+    const int rc = sym_eig(N, a, w);
+    *e0 = w[0];
+    for (int i = 0; i < N; ++i) phi[i] = a[i]; /* column 0 */
+    free(a);
+    free(w);
+    return rc;
+}
+
+/* Analysis::SCMF: grow the truncation p from 1 until the ground energy moves
+ * by at most eps = 10^-precision, set psi = sum_{i=1}^{2p} sqrt(i) phi_i
+ * phi_{i-1} (Analysis::SF_density), repeat until psi moves by at most eps.
+ * Returns psi (NaN if p would exceed pmax); *outer gets the psi updates. */
+double bho_scmf(double mu, double J, int q, double psi0, int precision, int pmax, int* outer) {
+    const double eps = pow(10.0, -precision);
+    double psi = psi0, tmp;
+    double* phi = (double*)malloc(sizeof(double) * (2 * pmax + 1));
+    int it = 0;
+    if (!phi) return NAN;
+    do {
+        int p = 1;
+        double e0, e1;
+        if (scmf_ground(psi, p, mu, J, q, phi, &e0)) {
+            free(phi);
+            return NAN;
+        }
+        do {
+            ++p;
+            if (p > pmax || scmf_ground(psi, p, mu, J, q, phi, &e1)) {
+                free(phi);
+                return NAN;
+            }
+            tmp = fabs(e0 - e1);
+            e0 = e1;
+        } while (tmp > eps);
+        double a = 0.0;
+        for (int i = 1; i < 2 * p + 1; ++i) a += sqrt((double)i) * phi[i] * phi[i - 1];
+        ++it;
+        tmp = fabs(a - psi);
+        psi = a;
+    } while (tmp > eps);
+    free(phi);
+    if (outer) *outer = it;
+    return psi;
+}
+
+/* bho_scmf over npts points in parallel (OpenMP); psi[k], outer[k]. */
+void bho_scmf_batch(int npts, const double* mu, const double* J, int q, const double* psi0,
+                    int precision, int pmax, int nthreads, double* psi, int* outer) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
+    for (int k = 0; k < npts; ++k) psi[k] = bho_scmf(mu[k], J[k], q, psi0[k], precision, pmax, outer ? &outer[k] : 0);
 }

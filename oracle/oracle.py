@@ -85,6 +85,11 @@ class Oracle:
         lib.bho_coherence.argtypes = [C.c_int, _f64p]
         lib.bho_condensate_fraction.restype = C.c_double
         lib.bho_condensate_fraction.argtypes = [C.c_int, _f64p]
+        lib.bho_scmf.restype = C.c_double
+        lib.bho_scmf.argtypes = [C.c_double, C.c_double, C.c_int, C.c_double, C.c_int, C.c_int,
+                                 C.c_void_p]
+        lib.bho_scmf_batch.argtypes = [C.c_int, _f64p, _f64p, C.c_int, _f64p, C.c_int, C.c_int,
+                                       C.c_int, _f64p, C.c_void_p]
 
     # ---- basis ----
     def dimension(self, m: int, n: int) -> int:
@@ -227,6 +232,22 @@ class Oracle:
         return float(self.lib.bho_condensate_fraction(rho.shape[0],
                                                       np.ascontiguousarray(rho.ravel())))
 
+    # ---- mean field ----
+    def scmf(self, mu, J, q, psi0, precision, pmax=64):
+        it = C.c_int(0)
+        v = self.lib.bho_scmf(mu, J, q, psi0, precision, pmax, C.byref(it))
+        return float(v), it.value
+
+    def scmf_batch(self, mu, J, q, psi0, precision, pmax=64, nthreads=0):
+        mu = np.ascontiguousarray(mu, np.float64)
+        J = np.ascontiguousarray(np.broadcast_to(J, mu.shape), np.float64)
+        psi0 = np.ascontiguousarray(np.broadcast_to(psi0, mu.shape), np.float64)
+        psi = np.zeros(len(mu))
+        outer = np.zeros(len(mu), np.int32)
+        self.lib.bho_scmf_batch(len(mu), mu, J, q, psi0, precision, pmax, nthreads, psi,
+                                outer.ctypes.data_as(C.c_void_p))
+        return psi, outer
+
 
 class Reference:
     """The reference's own exact-path code, compiled from its sources."""
@@ -244,6 +265,8 @@ class Reference:
         lib.ref_gap_ratios.argtypes = [C.c_int, _f64p, _f64p]
         lib.ref_coherence.restype = C.c_double
         lib.ref_coherence.argtypes = [C.c_int, _f64p]
+        lib.ref_scmf.restype = C.c_double
+        lib.ref_scmf.argtypes = [C.c_double, C.c_double, C.c_int, C.c_double, C.c_int]
 
     def fixed_set_basis(self, m, n):
         D = self.lib.ref_dimension(m, n)
@@ -294,3 +317,6 @@ class Reference:
 
     def coherence(self, rho):
         return float(self.lib.ref_coherence(rho.shape[0], np.ascontiguousarray(rho.ravel())))
+
+    def scmf(self, mu, J, q, psi0, precision):
+        return float(self.lib.ref_scmf(mu, J, q, psi0, precision))

@@ -132,4 +132,14 @@ double ref_coherence(int m, const double* rho) {
     return Analysis::coherence(s);
 }
 
+// Analysis::SCMF (analysis.cpp:111-178): the self-consistent mean-field order
+// parameter at (mu, J) from the seed psi0, eps = 10^-precision.
+double ref_scmf(double mu, double J, int q, double psi0, int precision) {
+    try {
+        return Analysis::SCMF(mu, J, q, psi0, precision);
+    } catch (const std::exception&) {
+        return std::nan("");
+    }
+}
+
 }  // extern "C"

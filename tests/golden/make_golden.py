@@ -11,8 +11,9 @@ oracle/Makefile into oracle/_ref/libbhref.so:
     assembled in the reference's column order by the CPU oracle (the
     reference's own builder is not a valid Hamiltonian: it loops over
     neighbour slots and reads out of bounds);
-  - Analysis::gap_ratios and Analysis::coherence.
-Usage:  python tests/golden/make_golden.py [--quick]
+  - Analysis::gap_ratios and Analysis::coherence;
+  - Analysis::SCMF (analysis.cpp:111-178), the mean-field order parameter.
+Usage:  python tests/golden/make_golden.py [--quick | --scmf-only]
 """
 from __future__ import annotations
 
@@ -174,11 +175,43 @@ def main(quick: bool):
     rho = rho + rho.T
     out["coherence"] = {"rho": rho.tolist(), "value": ref.coherence(rho)}
 
+    out["scmf"] = scmf_cases(ref)
+
     path = os.path.join(HERE, "reference_golden.json")
     with open(path, "w") as f:
         json.dump(out, f, indent=1)
     print("wrote", path, os.path.getsize(path), "bytes")
 
 
+def scmf_cases(ref):
+    """Analysis::SCMF (src/analysis.cpp:111-178) on a (mu, J) grid with fixed
+    seeds psi0 (the reference draws psi0 from std::random_device)."""
+    cases = []
+    rng = np.random.RandomState(11)
+    for q, prec in [(1, 6), (2, 8), (4, 7)]:
+        for mu in [0.1, 0.45, 0.9, 1.5, 2.3, 3.1, 3.8]:
+            for J in [0.01, 0.04, 0.09, 0.16, 0.24]:
+                psi0 = float(rng.uniform(0.05, 1.0))
+                cases.append({"mu": mu, "J": J, "q": q, "psi0": psi0, "precision": prec,
+                              "psi": ref.scmf(mu, J, q, psi0, prec)})
+    return cases
+
+
+def update_scmf_only():
+    """Adds or replaces only the scmf section of the committed fixture."""
+    orc.build_ref()
+    ref = orc.Reference()
+    path = os.path.join(HERE, "reference_golden.json")
+    with open(path) as f:
+        out = json.load(f)
+    out["scmf"] = scmf_cases(ref)
+    with open(path, "w") as f:
+        json.dump(out, f, indent=1)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
 if __name__ == "__main__":
-    main("--quick" in sys.argv)
+    if "--scmf-only" in sys.argv:
+        update_scmf_only()
+    else:
+        main("--quick" in sys.argv)
