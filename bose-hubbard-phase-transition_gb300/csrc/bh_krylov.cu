@@ -44,218 +44,6 @@ namespace bh {
 // kernels
 // ---------------------------------------------------------------------------
 
-// Y = H X for ncols columns; column t belongs to solve t / group with
-// prm[3 s + 0..2] = (J, U, shift).  L lanes per row, lanes over columns.
-template <class T, int L>
-__global__ void __launch_bounds__(256)
-k_spmm(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
-       const T* __restrict__ X, T* __restrict__ Y) {
-    const int gl = threadIdx.x % L;
-    const int rows_per_block = blockDim.x / L;
-    const int cpl = ncols / L;
-    for (int64_t r = (int64_t)blockIdx.x * rows_per_block + threadIdx.x / L; r < A.D;
-         r += (int64_t)gridDim.x * rows_per_block) {
-        const int64_t e0 = A.rp[r], e1 = A.rp[r + 1];
-        const T d = A.vd ? A.vd[r] : T(0);
-        for (int c0 = 0; c0 < cpl; c0 += 8) {
-            T acc[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) acc[u] = T(0);
-            const int nc = min(8, cpl - c0);
-            for (int64_t e = e0; e < e1; ++e) {
-                const int64_t col = A.ci[e];
-                const T v = A.tv[e];
-                const T* xr = X + col * ncols + gl + c0 * L;
-#pragma unroll
-                for (int u = 0; u < 8; ++u)
-                    if (u < nc) acc[u] += v * xr[u * L];
-            }
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                if (u < nc) {
-                    const int t = gl + (c0 + u) * L;
-                    const int s = t / group;
-                    const T Jc = (T)prm[3 * s], Uc = (T)prm[3 * s + 1], sh = (T)prm[3 * s + 2];
-                    const T xv = X[r * ncols + t];
-                    Y[r * ncols + t] = Jc * acc[u] + (Uc * d + sh) * xv;
-                }
-            }
-        }
-    }
-}
-
-// Matrix-free Y = H X: the row of state r is regenerated from its packed
-// occupation string.  L lanes per row (lanes over columns, as k_spmm); lane l
-// of a row evaluates the directed bonds k = l, l + L, ... (slot k / L): for
-// bond (i, j) with n_i >= 1 the target state s - e_i + e_j has index
-//   r' = r + sum_{i <= t < j} (RT[t][suf_t + 1] - RT[t][suf_t])        (i < j)
-//   r' = r - sum_{j <= t < i} (RT[t][suf_t] - RT[t][suf_t - 1])        (i > j)
-// (suf_t = bosons on sites > t, the only suffix sums the hop changes) and the
-// amplitude -sqrt(n_i (n_j + 1)) comes from a table.  The row's lanes then
-// walk the bonds in order, exchanging (r', amplitude) by shuffles, and gather
-// the X rows.  V = 1/2 sum n (n - 1) is recomputed from the string.
-// Target index and amplitude of directed bond k of the state with index r,
-// occupations w and packed suffix sums sufp; c = -1 if site i is empty.
-template <class T>
-__device__ __forceinline__ void mf_hop(int k, uint64_t w, uint64_t sufp, int64_t r, int bits,
-                                       uint64_t mask, int n, const uint8_t* s_bd,
-                                       const uint32_t* s_rt, const T* s_sq, int64_t& c, T& v) {
-    const int i = s_bd[2 * k], j = s_bd[2 * k + 1];
-    const int ni = (int)((w >> (bits * i)) & mask);
-    c = -1;
-    v = T(0);
-    if (ni < 1) return;
-    const int nj = (int)((w >> (bits * j)) & mask);
-    int64_t rr = r;
-    if (i < j) {
-        for (int t = i; t < j; ++t) {
-            const int st = (int)((sufp >> (bits * t)) & mask);
-            rr += (int64_t)s_rt[t * (n + 1) + st + 1] - (int64_t)s_rt[t * (n + 1) + st];
-        }
-    } else {
-        for (int t = j; t < i; ++t) {
-            const int st = (int)((sufp >> (bits * t)) & mask);
-            rr -= (int64_t)s_rt[t * (n + 1) + st] - (int64_t)s_rt[t * (n + 1) + st - 1];
-        }
-    }
-    c = rr;
-    v = s_sq[ni * (nj + 1)];
-}
-
-template <class T, int L>
-__global__ void __launch_bounds__(256)
-k_spmm_mf(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
-          const T* __restrict__ X, T* __restrict__ Y) {
-    constexpr int SLOTS = L >= 4 ? 128 / L : 1;
-    extern __shared__ __align__(16) unsigned char s_raw[];
-    const int m = A.m, n = A.n, nb = A.nbonds, bits = A.bits;
-    const int nrt = (m - 1) * (n + 1), nsq = n * (n + 1) + 1;
-    T* s_sq = reinterpret_cast<T*>(s_raw);
-    uint32_t* s_rt = reinterpret_cast<uint32_t*>(s_raw + (((size_t)nsq * sizeof(T) + 15) & ~(size_t)15));
-    uint8_t* s_bd = reinterpret_cast<uint8_t*>(s_rt + nrt);
-    for (int i = threadIdx.x; i < nsq; i += blockDim.x) s_sq[i] = A.sq[i];
-    for (int i = threadIdx.x; i < nrt; i += blockDim.x) s_rt[i] = A.rt[i];
-    for (int i = threadIdx.x; i < 2 * nb; i += blockDim.x) s_bd[i] = A.bonds[i];
-    __syncthreads();
-    const uint64_t mask = (1ull << bits) - 1ull;
-    const int lane = threadIdx.x & 31;
-    const int gl = threadIdx.x % L;
-    const unsigned seg = L == 32 ? 0xffffffffu : (((1u << L) - 1u) << (lane & ~(L - 1)));
-    const int rows_per_block = blockDim.x / L;
-    const int cpl = ncols / L;
-    for (int64_t r = (int64_t)blockIdx.x * rows_per_block + threadIdx.x / L; r < A.D;
-         r += (int64_t)gridDim.x * rows_per_block) {
-        const uint64_t w = A.occ[r];
-        // suffix sums suf_t (t <= m - 2), packed like the occupations
-        uint64_t sufp = 0;
-        int suf = 0, v2 = 0;
-        for (int t = m - 1; t >= 0; --t) {
-            const int nt = (int)((w >> (bits * t)) & mask);
-            v2 += nt * (nt - 1);
-            if (t < m - 1) sufp |= (uint64_t)suf << (bits * t);
-            suf += nt;
-        }
-        const T d = (T)(0.5 * (double)v2);
-        int64_t col[SLOTS];
-        T amp[SLOTS];
-        if constexpr (L >= 4) {
-#pragma unroll
-            for (int sl = 0; sl < SLOTS; ++sl) {
-                const int k = sl * L + gl;
-                col[sl] = -1;
-                amp[sl] = T(0);
-                if (k < nb) mf_hop<T>(k, w, sufp, r, bits, mask, n, s_bd, s_rt, s_sq, col[sl], amp[sl]);
-            }
-        }
-        for (int c0 = 0; c0 < cpl; c0 += 8) {
-            T acc[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) acc[u] = T(0);
-            const int nc = min(8, cpl - c0);
-            if constexpr (L >= 4) {
-#pragma unroll
-                for (int sl = 0; sl < SLOTS; ++sl) {
-                    if (sl * L >= nb) break;
-                    for (int src = 0; src < L; ++src) {
-                        if (sl * L + src >= nb) break;
-                        const int64_t c = __shfl_sync(seg, col[sl], src, L);
-                        const T v = __shfl_sync(seg, amp[sl], src, L);
-                        if (c < 0) continue;
-                        const T* xr = X + c * ncols + gl + c0 * L;
-#pragma unroll
-                        for (int u = 0; u < 8; ++u)
-                            if (u < nc) acc[u] += v * xr[u * L];
-                    }
-                }
-            } else {
-                // one or two lanes per row: each lane evaluates every bond
-                for (int k = 0; k < nb; ++k) {
-                    int64_t c;
-                    T v;
-                    mf_hop<T>(k, w, sufp, r, bits, mask, n, s_bd, s_rt, s_sq, c, v);
-                    if (c < 0) continue;
-                    const T* xr = X + c * ncols + gl + c0 * L;
-#pragma unroll
-                    for (int u = 0; u < 8; ++u)
-                        if (u < nc) acc[u] += v * xr[u * L];
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                if (u < nc) {
-                    const int t = gl + (c0 + u) * L;
-                    const int s = t / group;
-                    const T Jc = (T)prm[3 * s], Uc = (T)prm[3 * s + 1], sh = (T)prm[3 * s + 2];
-                    const T xv = X[r * ncols + t];
-                    Y[r * ncols + t] = Jc * acc[u] + (Uc * d + sh) * xv;
-                }
-            }
-        }
-    }
-}
-
-// Launch of Y = H X on a CSR or matrix-free operator (L lanes per row over
-// the columns).  Returns the algorithmic bytes of the product.
-template <class T>
-static double launch_spmm(const OpView<T>& op, int ncols, int group, const double* prm, const T* X,
-                          T* Y, cudaStream_t st) {
-    const int64_t D = op.D;
-    int L = 1;
-    while (L < 32 && L * 2 <= ncols && ncols % (L * 2) == 0) L *= 2;
-    if (op.occ) {
-        BH_REQUIRE(op.nbonds <= 128, "matrix-free product: at most 128 directed bonds");
-        const int rpb = 256 / L;
-        int64_t g = (D + rpb - 1) / rpb;
-        g = std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)sm_count() * 16));
-        const int nsq = op.n * (op.n + 1) + 1;
-        const size_t smem = (((size_t)nsq * sizeof(T) + 15) & ~(size_t)15) +
-                            (size_t)(op.m - 1) * (op.n + 1) * sizeof(uint32_t) + 2 * (size_t)op.nbonds;
-        switch (L) {
-            case 1: k_spmm_mf<T, 1><<<(unsigned)g, 256, smem, st>>>(op, ncols, group, prm, X, Y); break;
-            case 2: k_spmm_mf<T, 2><<<(unsigned)g, 256, smem, st>>>(op, ncols, group, prm, X, Y); break;
-            case 4: k_spmm_mf<T, 4><<<(unsigned)g, 256, smem, st>>>(op, ncols, group, prm, X, Y); break;
-            case 8: k_spmm_mf<T, 8><<<(unsigned)g, 256, smem, st>>>(op, ncols, group, prm, X, Y); break;
-            case 16: k_spmm_mf<T, 16><<<(unsigned)g, 256, smem, st>>>(op, ncols, group, prm, X, Y); break;
-            default: k_spmm_mf<T, 32><<<(unsigned)g, 256, smem, st>>>(op, ncols, group, prm, X, Y); break;
-        }
-        return (double)D * 8.0 + 2.0 * (double)D * ncols * sizeof(T);
-    }
-    const int rpb = 256 / L;
-    int64_t g = (D + rpb - 1) / rpb;
-    g = std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)sm_count() * 16));
-    switch (L) {
-        case 1: k_spmm<T, 1><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y); break;
-        case 2: k_spmm<T, 2><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y); break;
-        case 4: k_spmm<T, 4><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y); break;
-        case 8: k_spmm<T, 8><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y); break;
-        case 16: k_spmm<T, 16><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y); break;
-        default: k_spmm<T, 32><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y); break;
-    }
-    const double nnz = (double)op.rp_nnz;
-    return nnz * (4.0 + sizeof(T)) + (double)(D + 1) * 8.0 + (op.vd ? (double)D * sizeof(T) : 0.0) +
-           2.0 * (double)D * ncols * sizeof(T);
-}
-
 // Partial sums of C_s[(j p + q)][q'] = sum_r V_j[r][s p + q] W[r][s p + q'] over
 // one chunk of rows (blockIdx.x) and JT blocks j (blockIdx.y).
 // part layout: [chunk][c < kcap][ncols]  (row c, column s p + q').

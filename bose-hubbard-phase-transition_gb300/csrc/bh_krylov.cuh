@@ -81,6 +81,21 @@ struct SolveResult {
     bool breakdown = false;
 };
 
+// Y = H X for ncols columns of T (CSR operator: MF = false; matrix-free:
+// MF = true), solve of column t = t / group, prm[3 s..] = (J, U, shift);
+// returns the algorithmic bytes.  Instantiated for float and double in
+// bh_spmm_{csr,mf}_{f32,f64}.cu.
+template <class T, bool MF>
+double launch_spmm_kind(const OpView<T>& op, int ncols, int group, const double* prm, const T* X,
+                        T* Y, cudaStream_t st);
+
+template <class T>
+inline double launch_spmm(const OpView<T>& op, int ncols, int group, const double* prm, const T* X,
+                          T* Y, cudaStream_t st) {
+    return op.occ ? launch_spmm_kind<T, true>(op, ncols, group, prm, X, Y, st)
+                  : launch_spmm_kind<T, false>(op, ncols, group, prm, X, Y, st);
+}
+
 // Y = H X (FP64) for ncols columns, solve of column t = t / group, prm[3 s..] = (J, U, shift).
 void apply_operator(const OpView<double>& op, int ncols, int group, const double* d_prm,
                     const double* d_X, double* d_Y, cudaStream_t st);

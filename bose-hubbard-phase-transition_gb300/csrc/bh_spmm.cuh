@@ -1,0 +1,289 @@
+// bh_spmm.cuh -- the sparse products Y = H X of the solver (CSR and
+// matrix-free), included by one translation unit per element type.
+#pragma once
+
+#include <algorithm>
+#include <cstdint>
+#include <type_traits>
+
+#include "bh_krylov.cuh"
+
+namespace bh {
+
+// Y = H X for ncols columns; column t belongs to solve t / group with
+// prm[3 s + 0..2] = (J, U, shift).  L lanes per row, lanes over columns.
+template <class T, int L, int CW>
+__global__ void __launch_bounds__(256)
+k_spmm(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
+       const T* __restrict__ X, T* __restrict__ Y) {
+    const int gl = threadIdx.x % L;
+    const int rows_per_block = blockDim.x / L;
+    const int cpl = ncols / L;
+    for (int64_t r = (int64_t)blockIdx.x * rows_per_block + threadIdx.x / L; r < A.D;
+         r += (int64_t)gridDim.x * rows_per_block) {
+        const int64_t e0 = A.rp[r], e1 = A.rp[r + 1];
+        const T d = A.vd ? A.vd[r] : T(0);
+        for (int c0 = 0; c0 < cpl; c0 += CW) {
+            T acc[CW];
+#pragma unroll
+            for (int u = 0; u < CW; ++u) acc[u] = T(0);
+            const int nc = min(CW, cpl - c0);
+            // four entries per step: their X rows are all requested before the
+            // first product (the summation order per column is unchanged)
+            int64_t e = e0;
+            for (; e + 4 <= e1; e += 4) {
+                int64_t cc[4];
+                T vv[4], xv[4][CW];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    cc[k] = A.ci[e + k];
+                    vv[k] = A.tv[e + k];
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const T* xr = X + cc[k] * ncols + gl + c0 * L;
+#pragma unroll
+                    for (int u = 0; u < CW; ++u)
+                        if (u < nc) xv[k][u] = xr[u * L];
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+#pragma unroll
+                    for (int u = 0; u < CW; ++u)
+                        if (u < nc) acc[u] += vv[k] * xv[k][u];
+            }
+            for (; e < e1; ++e) {
+                const int64_t col = A.ci[e];
+                const T v = A.tv[e];
+                const T* xr = X + col * ncols + gl + c0 * L;
+#pragma unroll
+                for (int u = 0; u < CW; ++u)
+                    if (u < nc) acc[u] += v * xr[u * L];
+            }
+#pragma unroll
+            for (int u = 0; u < CW; ++u) {
+                if (u < nc) {
+                    const int t = gl + (c0 + u) * L;
+                    const int s = t / group;
+                    const T Jc = (T)prm[3 * s], Uc = (T)prm[3 * s + 1], sh = (T)prm[3 * s + 2];
+                    const T xv = X[r * ncols + t];
+                    Y[r * ncols + t] = Jc * acc[u] + (Uc * d + sh) * xv;
+                }
+            }
+        }
+    }
+}
+
+// Matrix-free Y = H X: the row of state r is regenerated from its packed
+// occupation string.  L lanes per row (lanes over columns, as k_spmm); lane l
+// of a row evaluates the directed bonds k = l, l + L, ... (slot k / L): for
+// bond (i, j) with n_i >= 1 the target state s - e_i + e_j has index
+//   r' = r + sum_{i <= t < j} (RT[t][suf_t + 1] - RT[t][suf_t])        (i < j)
+//   r' = r - sum_{j <= t < i} (RT[t][suf_t] - RT[t][suf_t - 1])        (i > j)
+// (suf_t = bosons on sites > t, the only suffix sums the hop changes) and the
+// amplitude -sqrt(n_i (n_j + 1)) comes from a table.  The row's lanes then
+// walk the bonds in order, exchanging (r', amplitude) by shuffles, and gather
+// the X rows.  V = 1/2 sum n (n - 1) is recomputed from the string.
+// Target index and amplitude of directed bond k of the state with index r,
+// occupations w and packed suffix sums sufp; c = -1 if site i is empty.
+template <class T>
+__device__ __forceinline__ void mf_hop(int k, uint64_t w, uint64_t sufp, int64_t r, int bits,
+                                       uint64_t mask, int n, const uint8_t* s_bd,
+                                       const uint32_t* s_rt, const T* s_sq, int64_t& c, T& v) {
+    const int i = s_bd[2 * k], j = s_bd[2 * k + 1];
+    const int ni = (int)((w >> (bits * i)) & mask);
+    c = -1;
+    v = T(0);
+    if (ni < 1) return;
+    const int nj = (int)((w >> (bits * j)) & mask);
+    int64_t rr = r;
+    if (i < j) {
+        for (int t = i; t < j; ++t) {
+            const int st = (int)((sufp >> (bits * t)) & mask);
+            rr += (int64_t)s_rt[t * (n + 1) + st + 1] - (int64_t)s_rt[t * (n + 1) + st];
+        }
+    } else {
+        for (int t = j; t < i; ++t) {
+            const int st = (int)((sufp >> (bits * t)) & mask);
+            rr -= (int64_t)s_rt[t * (n + 1) + st] - (int64_t)s_rt[t * (n + 1) + st - 1];
+        }
+    }
+    c = rr;
+    v = s_sq[ni * (nj + 1)];
+}
+
+template <class T, int L, int CW>
+__global__ void __launch_bounds__(256)
+k_spmm_mf(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
+          const T* __restrict__ X, T* __restrict__ Y) {
+    constexpr int SLOTS = L >= 4 ? 128 / L : 1;
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    const int m = A.m, n = A.n, nb = A.nbonds, bits = A.bits;
+    const int nrt = (m - 1) * (n + 1), nsq = n * (n + 1) + 1;
+    T* s_sq = reinterpret_cast<T*>(s_raw);
+    uint32_t* s_rt = reinterpret_cast<uint32_t*>(s_raw + (((size_t)nsq * sizeof(T) + 15) & ~(size_t)15));
+    uint8_t* s_bd = reinterpret_cast<uint8_t*>(s_rt + nrt);
+    // per-row hop lists (L >= 4): target index and amplitude of every bond
+    const size_t hop_off = (((size_t)nsq * sizeof(T) + 15) & ~(size_t)15) + (size_t)nrt * 4 + 2 * (size_t)nb;
+    int32_t* s_hc = reinterpret_cast<int32_t*>(s_raw + ((hop_off + 15) & ~(size_t)15));
+    T* s_hv = reinterpret_cast<T*>(s_hc + (blockDim.x / L) * nb + ((blockDim.x / L) * nb & 1));
+    for (int i = threadIdx.x; i < nsq; i += blockDim.x) s_sq[i] = A.sq[i];
+    for (int i = threadIdx.x; i < nrt; i += blockDim.x) s_rt[i] = A.rt[i];
+    for (int i = threadIdx.x; i < 2 * nb; i += blockDim.x) s_bd[i] = A.bonds[i];
+    __syncthreads();
+    const uint64_t mask = (1ull << bits) - 1ull;
+    const int lane = threadIdx.x & 31;
+    const int gl = threadIdx.x % L;
+    const unsigned seg = L == 32 ? 0xffffffffu : (((1u << L) - 1u) << (lane & ~(L - 1)));
+    const int rows_per_block = blockDim.x / L;
+    const int cpl = ncols / L;
+    int32_t* hc = s_hc + (threadIdx.x / L) * nb;
+    T* hv = s_hv + (threadIdx.x / L) * nb;
+    for (int64_t r = (int64_t)blockIdx.x * rows_per_block + threadIdx.x / L; r < A.D;
+         r += (int64_t)gridDim.x * rows_per_block) {
+        const uint64_t w = A.occ[r];
+        // suffix sums suf_t (t <= m - 2), packed like the occupations
+        uint64_t sufp = 0;
+        int suf = 0, v2 = 0;
+        for (int t = m - 1; t >= 0; --t) {
+            const int nt = (int)((w >> (bits * t)) & mask);
+            v2 += nt * (nt - 1);
+            if (t < m - 1) sufp |= (uint64_t)suf << (bits * t);
+            suf += nt;
+        }
+        const T d = (T)(0.5 * (double)v2);
+        if constexpr (L >= 4) {
+            // the row's lanes split the bonds, then share them through shared memory
+#pragma unroll
+            for (int sl = 0; sl < SLOTS; ++sl) {
+                const int k = sl * L + gl;
+                if (k < nb) {
+                    int64_t c;
+                    T v;
+                    mf_hop<T>(k, w, sufp, r, bits, mask, n, s_bd, s_rt, s_sq, c, v);
+                    hc[k] = (int32_t)c;
+                    hv[k] = v;
+                }
+            }
+            __syncwarp(seg);
+        }
+        for (int c0 = 0; c0 < cpl; c0 += CW) {
+            T acc[CW];
+#pragma unroll
+            for (int u = 0; u < CW; ++u) acc[u] = T(0);
+            const int nc = min(CW, cpl - c0);
+            if constexpr (L >= 4) {
+                // bonds in order, four per step: the four X rows are requested
+                // before the first product
+                for (int k0 = 0; k0 < nb; k0 += 4) {
+                    int32_t cc[4];
+                    T vv[4], xv[4][CW];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        cc[k] = k0 + k < nb ? hc[k0 + k] : -1;
+                        vv[k] = k0 + k < nb ? hv[k0 + k] : T(0);
+                    }
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        if (cc[k] < 0) continue;
+                        const T* xr = X + (int64_t)cc[k] * ncols + gl + c0 * L;
+#pragma unroll
+                        for (int u = 0; u < CW; ++u)
+                            if (u < nc) xv[k][u] = xr[u * L];
+                    }
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        if (cc[k] < 0) continue;
+#pragma unroll
+                        for (int u = 0; u < CW; ++u)
+                            if (u < nc) acc[u] += vv[k] * xv[k][u];
+                    }
+                }
+            } else {
+                // one or two lanes per row: each lane evaluates every bond
+                for (int k = 0; k < nb; ++k) {
+                    int64_t c;
+                    T v;
+                    mf_hop<T>(k, w, sufp, r, bits, mask, n, s_bd, s_rt, s_sq, c, v);
+                    if (c < 0) continue;
+                    const T* xr = X + c * ncols + gl + c0 * L;
+#pragma unroll
+                    for (int u = 0; u < CW; ++u)
+                        if (u < nc) acc[u] += v * xr[u * L];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < CW; ++u) {
+                if (u < nc) {
+                    const int t = gl + (c0 + u) * L;
+                    const int s = t / group;
+                    const T Jc = (T)prm[3 * s], Uc = (T)prm[3 * s + 1], sh = (T)prm[3 * s + 2];
+                    const T xv = X[r * ncols + t];
+                    Y[r * ncols + t] = Jc * acc[u] + (Uc * d + sh) * xv;
+                }
+            }
+        }
+        if constexpr (L >= 4) __syncwarp(seg);  // the next row overwrites the hop list
+    }
+}
+
+// Launch of Y = H X on a CSR (MF = false) or matrix-free (MF = true)
+// operator: L lanes per row over the columns (the largest power of two <= 32
+// dividing ncols), CW columns per lane per pass (1 or 2 when that covers the
+// row's share, else 4 with further passes).  For L < 32 the share ncols / L
+// is odd, so only CW in {1, 4} occurs there.  Returns the algorithmic bytes.
+template <class T, bool MF>
+double launch_spmm_kind(const OpView<T>& op, int ncols, int group, const double* prm, const T* X,
+                        T* Y, cudaStream_t st) {
+    const int64_t D = op.D;
+    int L = 1;
+    while (L < 32 && L * 2 <= ncols && ncols % (L * 2) == 0) L *= 2;
+    const int cpl = ncols / L;
+    int CW = cpl > 2 ? 4 : cpl;
+    if (L < 32 && CW == 2) CW = 4;
+    const int rpb = 256 / L;
+    int64_t g = (D + rpb - 1) / rpb;
+    g = std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)sm_count() * 16));
+    size_t smem = 0;
+    if (MF) {
+        BH_REQUIRE(op.nbonds <= 128, "matrix-free product: at most 128 directed bonds");
+        const int nsq = op.n * (op.n + 1) + 1;
+        smem = (((size_t)nsq * sizeof(T) + 15) & ~(size_t)15) +
+               (size_t)(op.m - 1) * (op.n + 1) * sizeof(uint32_t) + 2 * (size_t)op.nbonds;
+        if (L >= 4) {  // hop lists: (256 / L) rows x nbonds x (int32 + T), 16-byte aligned parts
+            const size_t nh = (size_t)(256 / L) * op.nbonds;
+            smem = ((smem + 15) & ~(size_t)15) + (nh + (nh & 1)) * 4 + nh * sizeof(T);
+        }
+    }
+    auto go = [&](auto lc, auto cwc) {
+        constexpr int LL = decltype(lc)::value, CC = decltype(cwc)::value;
+        if constexpr (MF) {
+            auto kern = k_spmm_mf<T, LL, CC>;
+            if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            kern<<<(unsigned)g, 256, smem, st>>>(op, ncols, group, prm, X, Y);
+        }
+        else k_spmm<T, LL, CC><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y);
+    };
+    auto odd_share = [&](auto lc) {
+        if (CW == 1) go(lc, std::integral_constant<int, 1>());
+        else go(lc, std::integral_constant<int, 4>());
+    };
+    switch (L) {
+        case 1: odd_share(std::integral_constant<int, 1>()); break;
+        case 2: odd_share(std::integral_constant<int, 2>()); break;
+        case 4: odd_share(std::integral_constant<int, 4>()); break;
+        case 8: odd_share(std::integral_constant<int, 8>()); break;
+        case 16: odd_share(std::integral_constant<int, 16>()); break;
+        default:
+            if (CW == 1) go(std::integral_constant<int, 32>(), std::integral_constant<int, 1>());
+            else if (CW == 2) go(std::integral_constant<int, 32>(), std::integral_constant<int, 2>());
+            else go(std::integral_constant<int, 32>(), std::integral_constant<int, 4>());
+            break;
+    }
+    if (MF) return (double)D * 8.0 + 2.0 * (double)D * ncols * sizeof(T);
+    const double nnz = (double)op.rp_nnz;
+    return nnz * (4.0 + sizeof(T)) + (double)(D + 1) * 8.0 + (op.vd ? (double)D * sizeof(T) : 0.0) +
+           2.0 * (double)D * ncols * sizeof(T);
+}
+
+}  // namespace bh

@@ -1,0 +1,8 @@
+// bh_spmm_mf_f32.cu -- the matrix-free Y = H X kernels for float vectors (see
+// bh_spmm.cuh); one translation unit per (operator kind, type) so they build in parallel.
+#include "bh_spmm.cuh"
+
+namespace bh {
+template double launch_spmm_kind<float, true>(const OpView<float>&, int, int, const double*, const float*,
+                                          float*, cudaStream_t);
+}  // namespace bh
