@@ -1011,6 +1011,17 @@ static bool verbose() {
 
 // BH_DEBUG_ORTHO=1 additionally measures the orthogonality of the Krylov basis
 // of the first active solve at every restart (diagnostic; costs one Gram pass).
+// BH_SEPARATE_LOCAL_DOT=1: compute the local coefficient with its own
+// reduction kernel instead of inside the SpMM (for comparing the two paths)
+static bool separate_local_dot() {
+    static int v = -1;
+    if (v < 0) {
+        const char* e = std::getenv("BH_SEPARATE_LOCAL_DOT");
+        v = (e && *e && *e != '0') ? 1 : 0;
+    }
+    return v == 1;
+}
+
 static bool debug_ortho() {
     static int v = -1;
     if (v < 0) {
@@ -1097,9 +1108,10 @@ struct Launcher {
         profile_end(st, name, bytes);
     }
 
-    void spmm(int ncols, int group, const double* prm, const T* X, T* Y) const {
+    void spmm(int ncols, int group, const double* prm, const T* X, T* Y, double* dpart = nullptr,
+              int* dparts = nullptr) const {
         profile_begin(st);
-        const double bytes = launch_spmm<T>(op, ncols, group, prm, X, Y, st);
+        const double bytes = launch_spmm<T>(op, ncols, group, prm, X, Y, st, dpart, dparts);
         done(op.occ ? "k_spmm_mf" : "k_spmm", bytes);
     }
 
@@ -1353,7 +1365,10 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
     // Va: basis (nb blocks + residual block).  Vb: restart target, and scratch
     // for the CholQR2 intermediate while a segment runs.
     DevBuf<T> Va((size_t)(nb + 1) * bmax), Vb((size_t)(nb + 1) * bmax), W((size_t)bmax);
-    DevBuf<double> part((size_t)nch_max * kcap * S0 * p), gpart((size_t)nchu_max * p * S0 * p);
+    // part: chunk partials of the projections, and of the local coefficient
+    // fused into the SpMM (at most 4 SM chunks of p rows)
+    const size_t part_rows = std::max((size_t)nch_max * kcap, (size_t)4 * sm_count() * p);
+    DevBuf<double> part(part_rows * S0 * p), gpart((size_t)nchu_max * p * S0 * p);
     DevBuf<T> Cf((size_t)kcap * S0 * p);
     DevBuf<double> Rinv((size_t)3 * S0 * p * p), Racc((size_t)S0 * p * p), Tm((size_t)S0 * Tdim * Tdim),
         d_prm((size_t)3 * S0);
@@ -1461,12 +1476,20 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
         const Geo g = make_geo(D, ncols), gu = make_ugeo(D, ncols);
         for (int j = jstart; j < nb; ++j) {
             T* Vj = Va.p + (int64_t)j * bstride;
-            L.spmm(ncols, p, d_prm.p, Vj, W.p);
+            // W = H V_j, with the partials of A = V_j^T W fused in where possible
+            int dparts = 0;
+            L.spmm(ncols, p, d_prm.p, Vj, W.p, separate_local_dot() ? nullptr : part.p, &dparts);
             res.matvecs += p;
             // local step: A = V_j^T W, then W -= V_j A + earlier couplings
             const int c_lo = (j == jstart && after_restart) ? 0 : std::max(0, (j - 1) * p);
-            L.dot(g, ncols, p, 1, bstride, Vj, W.p, kcap, part.p);
-            L.local_coef(g, j, c_lo, p, kcap, part.p, Tm.p, Tdim, Cf.p);
+            if (dparts > 0) {
+                Geo gs = g;
+                gs.nchunks = dparts;
+                L.local_coef(gs, j, c_lo, p, p, part.p, Tm.p, Tdim, Cf.p);
+            } else {
+                L.dot(g, ncols, p, 1, bstride, Vj, W.p, kcap, part.p);
+                L.local_coef(g, j, c_lo, p, kcap, part.p, Tm.p, Tdim, Cf.p);
+            }
             L.update(gu, p, (j + 1) * p - c_lo, bstride, Va.p + (int64_t)(c_lo / p) * bstride, Cf.p,
                      W.p, 0, gpart.p, "k_update(local)");
             // one full re-orthogonalisation pass, Gram matrix of the result

@@ -85,15 +85,19 @@ struct SolveResult {
 // MF = true), solve of column t = t / group, prm[3 s..] = (J, U, shift);
 // returns the algorithmic bytes.  Instantiated for float and double in
 // bh_spmm_{csr,mf}_{f32,f64}.cu.
+// With dpart (CSR operators, block size group = 2 or 4, at most one pass over
+// the row's columns) the product also writes the partial sums of X_s^T Y_s,
+// dpart[(chunk group + q) ncols + t] for chunk < *dparts; *dparts = 0 when
+// the product could not fuse them.
 template <class T, bool MF>
 double launch_spmm_kind(const OpView<T>& op, int ncols, int group, const double* prm, const T* X,
-                        T* Y, cudaStream_t st);
+                        T* Y, cudaStream_t st, double* dpart, int* dparts);
 
 template <class T>
 inline double launch_spmm(const OpView<T>& op, int ncols, int group, const double* prm, const T* X,
-                          T* Y, cudaStream_t st) {
-    return op.occ ? launch_spmm_kind<T, true>(op, ncols, group, prm, X, Y, st)
-                  : launch_spmm_kind<T, false>(op, ncols, group, prm, X, Y, st);
+                          T* Y, cudaStream_t st, double* dpart = nullptr, int* dparts = nullptr) {
+    return op.occ ? launch_spmm_kind<T, true>(op, ncols, group, prm, X, Y, st, dpart, dparts)
+                  : launch_spmm_kind<T, false>(op, ncols, group, prm, X, Y, st, dpart, dparts);
 }
 
 // Y = H X (FP64) for ncols columns, solve of column t = t / group, prm[3 s..] = (J, U, shift).

@@ -12,13 +12,33 @@ namespace bh {
 
 // Y = H X for ncols columns; column t belongs to solve t / group with
 // prm[3 s + 0..2] = (J, U, shift).  L lanes per row, lanes over columns.
-template <class T, int L, int CW>
+// DP > 0 (= group, one pass over the row's columns): the product also yields
+// the partial sums of X_s^T Y_s (the block-Lanczos coefficient A = V_j^T H V_j
+// of every solve): lane t holds Y[r][t] and receives X[r][s DP + q] from the
+// neighbouring lanes by shuffles; FP32 sums over 16 rows, then FP64 slots in
+// shared memory, reduced per CTA into dpart[(cta DP + q) ncols + t].
+template <class T, int L, int CW, int DP>
 __global__ void __launch_bounds__(256)
 k_spmm(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
-       const T* __restrict__ X, T* __restrict__ Y) {
+       const T* __restrict__ X, T* __restrict__ Y, double* __restrict__ dpart) {
+    extern __shared__ double s_dot[];
     const int gl = threadIdx.x % L;
+    const int lane = threadIdx.x & 31;
+    const unsigned seg = L == 32 ? 0xffffffffu : (((1u << L) - 1u) << (lane & ~(L - 1)));
     const int rows_per_block = blockDim.x / L;
     const int cpl = ncols / L;
+    constexpr int NDP = DP > 0 ? DP : 1;
+    T dacc[CW][NDP];
+    int drows = 0;
+    if constexpr (DP > 0) {
+#pragma unroll
+        for (int u = 0; u < CW; ++u)
+#pragma unroll
+            for (int q = 0; q < NDP; ++q) {
+                dacc[u][q] = T(0);
+                s_dot[(size_t)(u * NDP + q) * blockDim.x + threadIdx.x] = 0.0;
+            }
+    }
     for (int64_t r = (int64_t)blockIdx.x * rows_per_block + threadIdx.x / L; r < A.D;
          r += (int64_t)gridDim.x * rows_per_block) {
         const int64_t e0 = A.rp[r], e1 = A.rp[r + 1];
@@ -60,30 +80,63 @@ k_spmm(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
                 for (int u = 0; u < CW; ++u)
                     if (u < nc) acc[u] += v * xr[u * L];
             }
+            T xself[CW], yv[CW];
 #pragma unroll
             for (int u = 0; u < CW; ++u) {
+                xself[u] = T(0);
+                yv[u] = T(0);
                 if (u < nc) {
                     const int t = gl + (c0 + u) * L;
                     const int s = t / group;
                     const T Jc = (T)prm[3 * s], Uc = (T)prm[3 * s + 1], sh = (T)prm[3 * s + 2];
-                    const T xv = X[r * ncols + t];
-                    Y[r * ncols + t] = Jc * acc[u] + (Uc * d + sh) * xv;
+                    xself[u] = X[r * ncols + t];
+                    yv[u] = Jc * acc[u] + (Uc * d + sh) * xself[u];
+                    Y[r * ncols + t] = yv[u];
                 }
             }
+            if constexpr (DP > 0) {
+                const int qo = gl % DP;  // this lane's column within its solve
+#pragma unroll
+                for (int u = 0; u < CW; ++u)
+#pragma unroll
+                    for (int q = 0; q < DP; ++q) {
+                        const T xq = __shfl_sync(seg, xself[u], gl - qo + q, L);
+                        dacc[u][q] += xq * yv[u];
+                    }
+            }
+        }
+        if constexpr (DP > 0) {
+            if (++drows == 16) {
+                drows = 0;
+#pragma unroll
+                for (int u = 0; u < CW; ++u)
+#pragma unroll
+                    for (int q = 0; q < NDP; ++q) {
+                        s_dot[(size_t)(u * NDP + q) * blockDim.x + threadIdx.x] += (double)dacc[u][q];
+                        dacc[u][q] = T(0);
+                    }
+            }
+        }
+    }
+    if constexpr (DP > 0) {
+#pragma unroll
+        for (int u = 0; u < CW; ++u)
+#pragma unroll
+            for (int q = 0; q < NDP; ++q)
+                s_dot[(size_t)(u * NDP + q) * blockDim.x + threadIdx.x] += (double)dacc[u][q];
+        __syncthreads();
+        // one thread per (column t, q): sum over the CTA's row slots in order
+        for (int e = threadIdx.x; e < ncols * DP; e += blockDim.x) {
+            const int t = e / DP, q = e % DP;
+            const int u = t / L, g = t % L;
+            double sum = 0.0;
+            for (int ro = 0; ro < rows_per_block; ++ro)
+                sum += s_dot[(size_t)(u * NDP + q) * blockDim.x + ro * L + g];
+            dpart[((size_t)blockIdx.x * DP + q) * ncols + t] = sum;
         }
     }
 }
 
-// Matrix-free Y = H X: the row of state r is regenerated from its packed
-// occupation string.  L lanes per row (lanes over columns, as k_spmm); lane l
-// of a row evaluates the directed bonds k = l, l + L, ... (slot k / L): for
-// bond (i, j) with n_i >= 1 the target state s - e_i + e_j has index
-//   r' = r + sum_{i <= t < j} (RT[t][suf_t + 1] - RT[t][suf_t])        (i < j)
-//   r' = r - sum_{j <= t < i} (RT[t][suf_t] - RT[t][suf_t - 1])        (i > j)
-// (suf_t = bosons on sites > t, the only suffix sums the hop changes) and the
-// amplitude -sqrt(n_i (n_j + 1)) comes from a table.  The row's lanes then
-// walk the bonds in order, exchanging (r', amplitude) by shuffles, and gather
-// the X rows.  V = 1/2 sum n (n - 1) is recomputed from the string.
 // Target index and amplitude of directed bond k of the state with index r,
 // occupations w and packed suffix sums sufp; c = -1 if site i is empty.
 template <class T>
@@ -234,7 +287,7 @@ k_spmm_mf(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
 // is odd, so only CW in {1, 4} occurs there.  Returns the algorithmic bytes.
 template <class T, bool MF>
 double launch_spmm_kind(const OpView<T>& op, int ncols, int group, const double* prm, const T* X,
-                        T* Y, cudaStream_t st) {
+                        T* Y, cudaStream_t st, double* dpart, int* dparts) {
     const int64_t D = op.D;
     int L = 1;
     while (L < 32 && L * 2 <= ncols && ncols % (L * 2) == 0) L *= 2;
@@ -244,6 +297,13 @@ double launch_spmm_kind(const OpView<T>& op, int ncols, int group, const double*
     const int rpb = 256 / L;
     int64_t g = (D + rpb - 1) / rpb;
     g = std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)sm_count() * 16));
+    // fused X^T Y partials: CSR, one pass over the columns, block size 2 or 4
+    const bool fuse = !MF && dpart && (group == 2 || group == 4) && cpl <= CW && L >= group;
+    if (dparts) *dparts = 0;
+    if (fuse) {
+        g = std::min<int64_t>(g, (int64_t)sm_count() * 4);  // fewer partial rows to reduce
+        if (dparts) *dparts = (int)g;
+    }
     size_t smem = 0;
     if (MF) {
         BH_REQUIRE(op.nbonds <= 128, "matrix-free product: at most 128 directed bonds");
@@ -262,7 +322,11 @@ double launch_spmm_kind(const OpView<T>& op, int ncols, int group, const double*
             if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             kern<<<(unsigned)g, 256, smem, st>>>(op, ncols, group, prm, X, Y);
         }
-        else k_spmm<T, LL, CC><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y);
+        else if (fuse && group == 2)
+            k_spmm<T, LL, CC, 2><<<(unsigned)g, 256, 256 * CC * 2 * sizeof(double), st>>>(op, ncols, group, prm, X, Y, dpart);
+        else if (fuse && group == 4)
+            k_spmm<T, LL, CC, 4><<<(unsigned)g, 256, 256 * CC * 4 * sizeof(double), st>>>(op, ncols, group, prm, X, Y, dpart);
+        else k_spmm<T, LL, CC, 0><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y, nullptr);
     };
     auto odd_share = [&](auto lc) {
         if (CW == 1) go(lc, std::integral_constant<int, 1>());

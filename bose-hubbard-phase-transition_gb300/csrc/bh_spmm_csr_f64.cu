@@ -4,5 +4,5 @@
 
 namespace bh {
 template double launch_spmm_kind<double, false>(const OpView<double>&, int, int, const double*, const double*,
-                                          double*, cudaStream_t);
+                                          double*, cudaStream_t, double*, int*);
 }  // namespace bh

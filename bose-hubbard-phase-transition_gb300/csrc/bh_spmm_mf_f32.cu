@@ -4,5 +4,5 @@
 
 namespace bh {
 template double launch_spmm_kind<float, true>(const OpView<float>&, int, int, const double*, const float*,
-                                          float*, cudaStream_t);
+                                          float*, cudaStream_t, double*, int*);
 }  // namespace bh
