@@ -1011,6 +1011,17 @@ static bool verbose() {
 
 // BH_DEBUG_ORTHO=1 additionally measures the orthogonality of the Krylov basis
 // of the first active solve at every restart (diagnostic; costs one Gram pass).
+// BH_NO_GRAPHS=1: launch every kernel of a restart cycle directly instead of
+// replaying the captured cycle (for comparing the two)
+static bool use_graphs() {
+    static int v = -1;
+    if (v < 0) {
+        const char* e = std::getenv("BH_NO_GRAPHS");
+        v = (e && *e && *e != '0') ? 0 : 1;
+    }
+    return v == 1;
+}
+
 // BH_SEPARATE_LOCAL_DOT=1: compute the local coefficient with its own
 // reduction kernel instead of inside the SpMM (for comparing the two paths)
 static bool separate_local_dot() {
@@ -1470,10 +1481,23 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
     bool after_restart = false;
     int restarts = 0;
     const double eps23 = std::pow(2.220446049250313e-16, 2.0 / 3.0);
-    for (;;) {
-        const int ncols = S * p;
-        const int64_t bstride = D * ncols;
-        const Geo g = make_geo(D, ncols), gu = make_ugeo(D, ncols);
+    // The block steps jstart..nb-1 of a restart cycle launch the same kernels
+    // with the same arguments whenever the batch (S, jstart, after_restart) is
+    // unchanged, and need no host synchronisation: they are captured once as a
+    // CUDA graph and replayed (the slow last solves of a batch run many
+    // cycles at S = 1, where launch latency dominates).
+    // Va and Vb swap at every restart, so two graphs (one per buffer) are kept.
+    struct CycleGraph {
+        cudaGraphExec_t exec = nullptr;
+        int S = -1, jstart = -1;
+        bool after = false;
+        const T* va = nullptr;
+        int64_t launches = 0, matvecs = 0;
+        ~CycleGraph() {
+            if (exec) cudaGraphExecDestroy(exec);
+        }
+    } cgs[2];
+    auto run_steps = [&](int ncols, int64_t bstride, const Geo& g, const Geo& gu) {
         for (int j = jstart; j < nb; ++j) {
             T* Vj = Va.p + (int64_t)j * bstride;
             // W = H V_j, with the partials of A = V_j^T W fused in where possible
@@ -1498,6 +1522,49 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
             L.dot_finalize(g, kc, ncols, p, kcap, part.p, nullptr, Cf.p, Tm.p, Tdim, j);
             L.update(gu, p, kc, bstride, Va.p, Cf.p, W.p, 1, gpart.p);
             orthonormalize(gu, ncols, W.p, Va.p + (int64_t)(j + 1) * bstride, j + 1, true);
+        }
+    };
+    for (;;) {
+        const int ncols = S * p;
+        const int64_t bstride = D * ncols;
+        const Geo g = make_geo(D, ncols), gu = make_ugeo(D, ncols);
+        const bool graphs = after_restart && use_graphs() && !profile_on() && !debug_ortho();
+        CycleGraph& cg = cgs[restarts & 1];
+        if (graphs && cg.exec && cg.S == S && cg.jstart == jstart && cg.after == after_restart &&
+            cg.va == Va.p) {
+            BH_CUDA(cudaGraphLaunch(cg.exec, st));
+            res.launches += cg.launches;
+            res.matvecs += cg.matvecs;
+        } else if (graphs) {
+            if (cg.exec) {
+                BH_CUDA(cudaGraphExecDestroy(cg.exec));
+                cg.exec = nullptr;
+            }
+            const int64_t l0 = res.launches, m0 = res.matvecs;
+            cudaGraph_t graph = nullptr;
+            BH_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            try {
+                run_steps(ncols, bstride, g, gu);
+            } catch (...) {
+                cudaStreamEndCapture(st, &graph);
+                if (graph) cudaGraphDestroy(graph);
+                throw;
+            }
+            BH_CUDA(cudaStreamEndCapture(st, &graph));
+            cudaGraphExec_t exec = nullptr;
+            const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            BH_CUDA(e);
+            cg.exec = exec;
+            cg.S = S;
+            cg.jstart = jstart;
+            cg.after = after_restart;
+            cg.va = Va.p;
+            cg.launches = res.launches - l0;
+            cg.matvecs = res.matvecs - m0;
+            BH_CUDA(cudaGraphLaunch(cg.exec, st));
+        } else {
+            run_steps(ncols, bstride, g, gu);
         }
         if (debug_ortho()) {
             // Gram matrix of all nb + 1 blocks against each block, solve 0
