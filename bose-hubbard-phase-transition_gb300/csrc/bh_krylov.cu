@@ -1168,7 +1168,7 @@ struct Launcher {
                 else dotv_t<1, 8, 2>(g, nblk, bstride, V, W, kcap, part);
             } else if (p == 2) {
                 if (nblk == 1) dotv_t<2, 1, 4>(g, nblk, bstride, V, W, kcap, part);
-                else dotv_t<2, 4, 2>(g, nblk, bstride, V, W, kcap, part);
+                else dotv_t<2, 2, 4>(g, nblk, bstride, V, W, kcap, part);
             } else {
                 if (nblk == 1) dotv_t<4, 1, 2>(g, nblk, bstride, V, W, kcap, part);
                 else dotv_t<4, 2, 2>(g, nblk, bstride, V, W, kcap, part);
