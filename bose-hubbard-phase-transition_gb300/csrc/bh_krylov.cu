@@ -463,7 +463,7 @@ k_updatev(int64_t D, int S, int nblk, int64_t bstride, const T* __restrict__ V,
                 aA[q] = T(0);
                 aB[q] = T(0);
             }
-            constexpr int U = P >= 4 ? 2 : 4;  // blocks per inner step: 2 U vector loads in flight
+            constexpr int U = P >= 4 ? 4 : 8;  // blocks per inner step: 2 U vector loads in flight
             int j = 0;
             for (; j + U - 1 < nblk; j += U) {
                 Vec<T, P> x[U], y[U];
@@ -1280,7 +1280,8 @@ struct Launcher {
         constexpr int V4 = 16 / sizeof(T), E = 128 / sizeof(T);
         // outputs per pass (a template value below); Y rows padded to a whole
         // number of passes so that every pass reads inside its row
-        const int NO = sizeof(T) == 4 ? (nout <= 16 ? 16 : 24) : (nout <= 8 ? 8 : 16);
+        const int NO = sizeof(T) == 4 ? (nout <= 16 ? 16 : (nout <= 24 ? 24 : (nout <= 40 ? 40 : 48)))
+                                      : (nout <= 8 ? 8 : 16);
         const int npad = (nout + NO - 1) / NO * NO;
         const int ystride = ((kc * npad + E - 1) / E) * E + V4;
         const size_t per = (size_t)ystride * sizeof(T);
@@ -1309,11 +1310,15 @@ struct Launcher {
         };
         auto pick = [&](auto pv) {
             constexpr int PV = decltype(pv)::value;
-            // RB rows per thread: 4 on the FP32 vector path, else 1
+            // RB rows per thread: 4 on the FP32 vector path (2 with 40 or 48
+            // outputs per pass, which keeps a restart's outputs in one pass), else 1
             constexpr int RB = (sizeof(T) == 4 && PV >= 1) ? 4 : 1;
+            constexpr int RB48 = (sizeof(T) == 4 && PV >= 1) ? 2 : 1;
             if constexpr (sizeof(T) == 4) {
                 if (NO == 16) launch(k_rotate<T, 16, PV, RB>);
-                else launch(k_rotate<T, 24, PV, RB>);
+                else if (NO == 24) launch(k_rotate<T, 24, PV, RB>);
+                else if (NO == 40) launch(k_rotate<T, 40, PV, RB48>);
+                else launch(k_rotate<T, 48, PV, RB48>);
             } else {
                 if (NO == 8) launch(k_rotate<T, 8, PV, RB>);
                 else launch(k_rotate<T, 16, PV, RB>);
