@@ -57,7 +57,7 @@ EXPORTS = [
     "bh_hamiltonian_create_matrix_free", "bh_hamiltonian_is_matrix_free",
     "bh_hamiltonian_destroy", "bh_hamiltonian_nnz", "bh_hamiltonian_csr",
     "bh_hamiltonian_apply", "bh_hamiltonian_apply_noalloc", "bh_solver_opts_default", "bh_eigsh", "bh_eigsh_csr",
-    "bh_eigsh_batch", "bh_dense_eigh", "bh_gap_ratios", "bh_spdm", "bh_phase_map", "bh_scmf", "bh_mean_field_grid", "bh_profile_enable",
+    "bh_eigsh_batch", "bh_eigsh_batch_sectors", "bh_dense_eigh", "bh_gap_ratios", "bh_spdm", "bh_phase_map", "bh_scmf", "bh_mean_field_grid", "bh_profile_enable",
     "bh_profile_reset", "bh_profile_count", "bh_profile_get",
 ]
 
@@ -103,6 +103,8 @@ def load() -> C.CDLL:
                                C.POINTER(bh_solve_info)]
     L.bh_eigsh_batch.argtypes = [vp, C.c_int, vp, vp, vp, C.POINTER(bh_solver_opts), vp, vp, vp,
                                  C.POINTER(bh_solve_info)]
+    L.bh_eigsh_batch_sectors.argtypes = [C.c_int, vp, C.c_int, vp, vp, vp, C.POINTER(bh_solver_opts), vp, vp, vp,
+                                         C.POINTER(bh_solve_info)]
     L.bh_dense_eigh.argtypes = [C.c_int64, vp, vp, vp]
     L.bh_gap_ratios.argtypes = [C.c_int, vp, vp, f64p]
     L.bh_spdm.argtypes = [vp, C.c_int, vp, vp]
@@ -306,6 +308,27 @@ class Hamiltonian:
         rho = np.zeros(self.m * self.m)
         _check(load().bh_spdm(self._h, order, _ptr(phi), _ptr(rho)))
         return rho.reshape(self.m, self.m)
+
+
+def eigsh_sectors(hams, J, U, mu, nev: int = 10, **opt):
+    """Batched solve of the same (J, U, mu) points in several Hamiltonians
+    (particle-number sectors) at once, the sectors running concurrently on
+    the device (bh_eigsh_batch_sectors).  Returns ev, resid [nh, S, nev],
+    nconv [nh, S] and the aggregate SolveInfo."""
+    J = np.ascontiguousarray(J, np.float64)
+    S = len(J)
+    U = np.ascontiguousarray(np.broadcast_to(U, (S,)), np.float64)
+    mu = np.ascontiguousarray(np.broadcast_to(mu, (S,)), np.float64)
+    nh = len(hams)
+    o = default_opts(nev=nev, **opt)
+    hs = (C.c_void_p * nh)(*[h._h.value for h in hams])
+    ev = np.zeros((nh, S, nev))
+    rs = np.zeros((nh, S, nev))
+    nc = np.zeros((nh, S), np.int32)
+    info = bh_solve_info()
+    _check(load().bh_eigsh_batch_sectors(nh, C.cast(hs, C.c_void_p), S, _ptr(J), _ptr(U), _ptr(mu),
+                                         C.byref(o), _ptr(ev), _ptr(rs), _ptr(nc), C.byref(info)))
+    return ev, rs, nc, _info(info)
 
 
 def _info(i: bh_solve_info) -> SolveInfo:

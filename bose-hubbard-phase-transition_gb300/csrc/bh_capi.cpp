@@ -6,6 +6,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "bh_internal.h"
@@ -371,6 +372,74 @@ int bh_eigsh_batch(const bh_hamiltonian* h, int nsolve, const double* J, const d
         if (nconv) std::memcpy(nconv, r.nconv.data(), nsolve * sizeof(int));
         const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         fill_info(info, r, o->nev, secs);
+    });
+}
+
+int bh_eigsh_batch_sectors(int nh, const bh_hamiltonian* const* hs, int nsolve, const double* J,
+                           const double* U, const double* mu, const bh_solver_opts* o, double* evals,
+                           double* resid, int* nconv, bh_solve_info* info) {
+    return guard([&] {
+        const auto t0 = std::chrono::steady_clock::now();
+        BH_REQUIRE(nh >= 1 && hs && J && U && mu && evals, "null argument or nh < 1");
+        BH_REQUIRE(nsolve >= 1, "nsolve must be >= 1");
+        check_solver_opts(o);
+        for (int k = 0; k < nh; ++k) BH_REQUIRE(hs[k] != nullptr, "null Hamiltonian");
+        int dev = 0;
+        BH_CUDA(cudaGetDevice(&dev));
+        const int nev = o->nev;
+        std::vector<SolveResult> res(nh);
+        std::vector<int> codes(nh, BH_OK);
+        std::vector<std::string> msgs(nh);
+        // one host thread per sector, each with its own stream: the sectors'
+        // kernels overlap on the device, and one sector's restart work on the
+        // host (or its slowest last solve) leaves the GPU to the others
+        auto work = [&](int k) {
+            try {
+                BH_CUDA(cudaSetDevice(dev));
+                const bh_hamiltonian* h = hs[k];
+                SolveRequest rq = make_request(o, h->D, nsolve);
+                rq.want_vectors = false;
+                rq.d_perm = h->basis->d_col_of_lex.p;
+                rq.J.assign(J, J + nsolve);
+                rq.U.assign(U, U + nsolve);
+                rq.shift.resize(nsolve);
+                for (int s = 0; s < nsolve; ++s) rq.shift[s] = -mu[s] * (double)h->n;
+                Stream st;
+                res[k] = block_lanczos(op64_of(h), op32_of(h), rq, st);
+            } catch (const Error& e) {
+                codes[k] = e.code;
+                msgs[k] = e.what();
+            } catch (const std::bad_alloc&) {
+                codes[k] = BH_ERR_NOMEM;
+                msgs[k] = "host allocation failed";
+            } catch (const std::exception& e) {
+                codes[k] = BH_ERR_CUDA;
+                msgs[k] = e.what();
+            }
+        };
+        if (nh == 1 || profile_on()) {
+            for (int k = 0; k < nh; ++k) work(k);  // per-kernel timing wants no overlap
+        } else {
+            std::vector<std::thread> th;
+            for (int k = 0; k < nh; ++k) th.emplace_back(work, k);
+            for (auto& t : th) t.join();
+        }
+        for (int k = 0; k < nh; ++k)
+            if (codes[k] != BH_OK) throw Error(codes[k], "sector " + std::to_string(k) + ": " + msgs[k]);
+        SolveResult agg;
+        for (int k = 0; k < nh; ++k) {
+            const SolveResult& r = res[k];
+            std::memcpy(evals + (size_t)k * nsolve * nev, r.evals.data(), r.evals.size() * sizeof(double));
+            if (resid) std::memcpy(resid + (size_t)k * nsolve * nev, r.resid.data(), r.resid.size() * sizeof(double));
+            if (nconv) std::memcpy(nconv + (size_t)k * nsolve, r.nconv.data(), nsolve * sizeof(int));
+            agg.nconv.insert(agg.nconv.end(), r.nconv.begin(), r.nconv.end());
+            agg.resid.insert(agg.resid.end(), r.resid.begin(), r.resid.end());
+            agg.restarts = std::max(agg.restarts, r.restarts);
+            agg.matvecs += r.matvecs;
+            agg.launches += r.launches;
+        }
+        const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        fill_info(info, agg, nev, secs);
     });
 }
 

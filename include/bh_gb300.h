@@ -196,6 +196,16 @@ int bh_eigsh_csr(int64_t dim, const int64_t* row_ptr, const int32_t* col, const 
 int bh_eigsh_batch(const bh_hamiltonian* h, int nsolve, const double* J, const double* U,
                    const double* mu, const bh_solver_opts* o, double* evals, double* resid,
                    int* nconv, bh_solve_info* info);
+/* The same batch over nh Hamiltonians (the particle-number sectors of a
+ * phase diagram, of uneven dimension) in one call: the sectors run
+ * concurrently on the device, each on its own stream driven by its own host
+ * thread (sequentially while per-kernel timing is on).  mu is applied as
+ * -mu[s] * n_k in sector k.  evals[(k*nsolve + s)*nev + i], resid likewise,
+ * nconv[k*nsolve + s]; info aggregates (matvecs and launches summed,
+ * restarts = the largest of the sectors). */
+int bh_eigsh_batch_sectors(int nh, const bh_hamiltonian* const* hs, int nsolve, const double* J,
+                           const double* U, const double* mu, const bh_solver_opts* o,
+                           double* evals, double* resid, int* nconv, bh_solve_info* info);
 
 /* Replaces Op::exact_eigen (operator.cpp:92-101): all eigenvalues (ascending)
  * and, if z != NULL, eigenvectors (columns of z, column-major n x n) of the
