@@ -558,13 +558,17 @@ __global__ void __launch_bounds__(QR_THREADS)
 k_qr_finalize(int p, int nchunks, int ncols, const double* __restrict__ gpart, int mode,
               double shift_rel, double* __restrict__ Racc, double* __restrict__ Rinv,
               double* __restrict__ Tm, int Tdim, int jrow, double kill_abs,
-              unsigned char* __restrict__ dead) {
+              unsigned char* __restrict__ dead, int* __restrict__ need3) {
     __shared__ double G[16][16];
     const int s = blockIdx.x;
     const int warp = threadIdx.x >> 5;
+    // final pass of a step whose blocks were all well conditioned: the middle
+    // Gram pass was skipped and the block is already orthonormal (G = I)
+    const bool skipped = mode == 2 && need3 && *need3 == 0;
     for (int e = warp; e < p * p; e += QR_THREADS / 32) {
         const int a = e / p, b = e % p;
-        const double v = warp_sum_chunks(gpart, nchunks, (size_t)p * ncols, (size_t)a * ncols + s * p + b);
+        const double v = skipped ? (a == b ? 1.0 : 0.0)
+                                 : warp_sum_chunks(gpart, nchunks, (size_t)p * ncols, (size_t)a * ncols + s * p + b);
         if ((threadIdx.x & 31) == 0) G[a][b] = v;
     }
     __syncthreads();
@@ -576,24 +580,41 @@ k_qr_finalize(int p, int nchunks, int ncols, const double* __restrict__ gpart, i
             Ri[a][b] = 0.0;
             Rt[a][b] = 0.0;
         }
-    double shift = 0.0;
+    double* Ra = Racc + (size_t)s * p * p;
+    auto cholesky = [&](double shift) {
+        double dmin = INFINITY;
+        for (int i = 0; i < p; ++i) {
+            double d = G[i][i] + shift;
+            for (int k = 0; k < i; ++k) d -= R[k][i] * R[k][i];
+            dmin = fmin(dmin, d);
+            R[i][i] = 0.0;
+            for (int j = i + 1; j < p; ++j) R[i][j] = 0.0;
+            if (!(d > 0.0)) continue;  // zero column (already dropped) stays zero
+            const double rii = sqrt(d);
+            R[i][i] = rii;
+            for (int j = i + 1; j < p; ++j) {
+                double v = 0.5 * (G[i][j] + G[j][i]);
+                for (int k = 0; k < i; ++k) v -= R[k][i] * R[k][j];
+                R[i][j] = v / rii;
+            }
+        }
+        return dmin;
+    };
     if (mode == 0) {
         double gmax = 0.0;
         for (int i = 0; i < p; ++i) gmax = fmax(gmax, G[i][i]);
-        shift = shift_rel * gmax;
-    }
-    double* Ra = Racc + (size_t)s * p * p;
-    for (int i = 0; i < p; ++i) {
-        double d = G[i][i] + shift;
-        for (int k = 0; k < i; ++k) d -= R[k][i] * R[k][i];
-        if (!(d > 0.0)) continue;  // zero column (already dropped) stays zero
-        const double rii = sqrt(d);
-        R[i][i] = rii;
-        for (int j = i + 1; j < p; ++j) {
-            double v = 0.5 * (G[i][j] + G[j][i]);
-            for (int k = 0; k < i; ++k) v -= R[k][i] * R[k][j];
-            R[i][j] = v / rii;
+        // well conditioned (every pivot >= 1e-4 of the largest diagonal
+        // entry, i.e. cond(W)^2 <= 1e4): plain Cholesky, and two passes
+        // (CholQR2) orthonormalise to working precision.  Otherwise the
+        // shifted first pass, and the step needs all three.
+        bool plain = need3 != nullptr && gmax > 0.0;
+        if (plain) plain = cholesky(0.0) >= 1e-4 * gmax;
+        if (!plain) {
+            cholesky(shift_rel * gmax);
+            if (need3) atomicAdd(need3, 1);
         }
+    } else {
+        cholesky(0.0);
     }
     // accumulated factor Rt = R * Racc (upper triangular products)
     for (int a = 0; a < p; ++a)
@@ -674,8 +695,11 @@ template <class T, int P>
 __global__ void __launch_bounds__(256)
 k_normgram(int64_t D, int S, int nR, const double* __restrict__ Rinv, int64_t rstride,
            const T* __restrict__ W, T* __restrict__ Vout, int64_t rows_per_cta, int do_gram,
-           double* __restrict__ gpart) {
+           double* __restrict__ gpart, const int* __restrict__ skip_if_zero, int* __restrict__ reset) {
     extern __shared__ double sG[];
+    // a pass the step does not need (all blocks well conditioned) does nothing
+    if (skip_if_zero && *skip_if_zero == 0) return;
+    if (reset && blockIdx.x == 0 && threadIdx.x == 0) *reset = 0;
     constexpr int RU = 4;
     const int ncols = S * P;
     const int s = threadIdx.x % S, ro = threadIdx.x / S, R = blockDim.x / S;
@@ -1242,30 +1266,32 @@ struct Launcher {
     }
     void qr(const Geo& gu, int S, int p, const double* gpart, int mode, double shift_rel,
             double* Racc, double* Rinv, double* Tm, int Tdim, int jrow, double kill_abs,
-            unsigned char* dead) const {
+            unsigned char* dead, int* need3 = nullptr) const {
         profile_begin(st);
         k_qr_finalize<<<S, QR_THREADS, 0, st>>>(p, gu.nchunks, gu.ncols, gpart, mode, shift_rel, Racc,
-                                                Rinv, Tm, Tdim, jrow, kill_abs, dead);
+                                                Rinv, Tm, Tdim, jrow, kill_abs, dead, need3);
         done("k_qr_finalize", (double)gu.nchunks * p * gu.ncols * 8.0);
     }
     template <int P>
     void normgram_t(const Geo& g, int nR, const double* Rinv, int64_t rstride, const T* W, T* Vout,
-                    int do_gram, double* gpart) const {
+                    int do_gram, double* gpart, const int* skip_if_zero, int* reset) const {
         const int S = g.ncols / P;
         const int NT = S * std::max(1, 256 / S);
         const size_t smem = do_gram ? (size_t)NT * P * P * sizeof(double) : 0;
         auto kern = k_normgram<T, P>;
         if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         profile_begin(st);
-        kern<<<g.nchunks, NT, smem, st>>>(op.D, S, nR, Rinv, rstride, W, Vout, g.rows_per_chunk, do_gram, gpart);
+        kern<<<g.nchunks, NT, smem, st>>>(op.D, S, nR, Rinv, rstride, W, Vout, g.rows_per_chunk, do_gram, gpart,
+                                          skip_if_zero, reset);
         done(Vout ? "k_normalize" : "k_gram", (double)op.D * g.ncols * sizeof(T) * (Vout ? 2.0 : 1.0));
     }
     // nR factors applied to W; result to Vout (optional) and/or its Gram partials
+    // skip_if_zero: the pass does nothing when *skip_if_zero == 0; reset: set to 0 by the pass
     void normgram(const Geo& g, int p, int nR, const double* Rinv, int64_t rstride, const T* W, T* Vout,
-                  int do_gram, double* gpart) const {
-        if (p == 1) normgram_t<1>(g, nR, Rinv, rstride, W, Vout, do_gram, gpart);
-        else if (p == 2) normgram_t<2>(g, nR, Rinv, rstride, W, Vout, do_gram, gpart);
-        else normgram_t<4>(g, nR, Rinv, rstride, W, Vout, do_gram, gpart);
+                  int do_gram, double* gpart, const int* skip_if_zero = nullptr, int* reset = nullptr) const {
+        if (p == 1) normgram_t<1>(g, nR, Rinv, rstride, W, Vout, do_gram, gpart, skip_if_zero, reset);
+        else if (p == 2) normgram_t<2>(g, nR, Rinv, rstride, W, Vout, do_gram, gpart, skip_if_zero, reset);
+        else normgram_t<4>(g, nR, Rinv, rstride, W, Vout, do_gram, gpart, skip_if_zero, reset);
     }
     void normalize(int ncols, int p, const double* Rinv, const T* W, T* Vout) const {
         profile_begin(st);
@@ -1389,6 +1415,8 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
     DevBuf<double> Rinv((size_t)3 * S0 * p * p), Racc((size_t)S0 * p * p), Tm((size_t)S0 * Tdim * Tdim),
         d_prm((size_t)3 * S0);
     DevBuf<unsigned char> dead((size_t)S0 * Tdim);
+    DevBuf<int> need3(1);
+    BH_CUDA(cudaMemsetAsync(need3.p, 0, sizeof(int), st));
     DevBuf<int> d_in(S0), d_out(S0);
     DevBuf<T> Yd((size_t)S0 * kmax * kmax);
     Xout.alloc((size_t)D * S0 * K);
@@ -1430,12 +1458,14 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
                 L.normgram(gu, p, 1, Rinv.p, rs, Wb, Vout, 0, gpart.p);
                 return;
             }
-            L.qr(gu, S, p, gpart.p, 0, shift_rel, Racc.p, Rinv.p, nullptr, Tdim, jrow, kill_abs, nullptr);
+            // need3 counts the solves whose first pass needed the shift; when
+            // none did, the third pass is skipped on the device (CholQR2)
+            L.qr(gu, S, p, gpart.p, 0, shift_rel, Racc.p, Rinv.p, nullptr, Tdim, jrow, kill_abs, nullptr, need3.p);
             L.normgram(gu, p, 1, Rinv.p, rs, Wb, nullptr, 1, gpart.p);
             L.qr(gu, S, p, gpart.p, 1, 0.0, Racc.p, Rinv.p + rs, nullptr, Tdim, jrow, kill_abs, nullptr);
-            L.normgram(gu, p, 2, Rinv.p, rs, Wb, nullptr, 1, gpart.p);
-            L.qr(gu, S, p, gpart.p, 2, 0.0, Racc.p, Rinv.p + 2 * rs, Tj, Tdim, jrow, kill_abs, dead.p);
-            L.normgram(gu, p, 3, Rinv.p, rs, Wb, Vout, 0, gpart.p);
+            L.normgram(gu, p, 2, Rinv.p, rs, Wb, nullptr, 1, gpart.p, need3.p);
+            L.qr(gu, S, p, gpart.p, 2, 0.0, Racc.p, Rinv.p + 2 * rs, Tj, Tdim, jrow, kill_abs, dead.p, need3.p);
+            L.normgram(gu, p, 3, Rinv.p, rs, Wb, Vout, 0, gpart.p, nullptr, need3.p);
             return;
         }
         if (!gram_done) L.update(gu, p, 0, 0, Va.p, Cf.p, Wb, 1, gpart.p);
@@ -1444,7 +1474,7 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
             L.normalize(ncols, p, Rinv.p, Wb, Vout);
             return;
         }
-        // shifted CholQR3: Wb -> scratch -> Wb -> Vout
+        // shifted CholQR3: Wb -> scratch -> Wb -> Vout (no device-side pass skipping here)
         L.qr(gu, S, p, gpart.p, 0, shift_rel, Racc.p, Rinv.p, nullptr, Tdim, jrow, kill_abs, nullptr);
         L.normalize(ncols, p, Rinv.p, Wb, scratch);
         L.update(gu, p, 0, 0, Va.p, Cf.p, scratch, 1, gpart.p);
