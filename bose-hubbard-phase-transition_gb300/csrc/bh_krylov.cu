@@ -787,6 +787,21 @@ k_normgram(int64_t D, int S, int nR, const double* __restrict__ Rinv, int64_t rs
     }
 }
 
+// Packed FP32 pairs for the rotation's FMAs: one fma.rn.f32x2 performs two
+// fused multiply-adds (each rounded to nearest, as the scalar form), halving
+// the FMA instructions of an issue-bound loop.
+__device__ __forceinline__ unsigned long long pack2(float lo, float hi) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void unpack2(unsigned long long v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ void fma2(unsigned long long& acc, unsigned long long x, unsigned long long y) {
+    asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(acc) : "l"(x), "l"(y));
+}
+
 // Ritz rotation: for the processed solves ls < Sproc (input solve in_idx[ls],
 // output slot out_idx[ls]):  out[:, i] = sum_{c < kc} V[:, c] Y_ls[c][i].
 // Input column c of solve s is V_{c/p}[r][s p + c%p] (row stride ld_in).
@@ -842,7 +857,55 @@ k_rotate(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t bstri
             for (int k = 0; k < RB; ++k)
 #pragma unroll
                 for (int u = 0; u < NO; ++u) acc[k][u] = T(0);
-            if constexpr (PV >= 1) {
+            if constexpr (PV >= 1 && std::is_same<T, float>::value && NO % 4 == 0) {
+                // FP32: accumulators as packed pairs, two outputs per FMA instruction
+                unsigned long long acc2[RB][NO / 2];
+#pragma unroll
+                for (int k = 0; k < RB; ++k)
+#pragma unroll
+                    for (int u = 0; u < NO / 2; ++u) acc2[k][u] = 0ull;
+                constexpr int UJ = PV == 1 ? 4 : 2;
+                for (int j = 0; j < nblk; j += UJ) {
+                    Vec<T, PV> x[UJ][RB];
+#pragma unroll
+                    for (int u = 0; u < UJ; ++u)
+#pragma unroll
+                        for (int k = 0; k < RB; ++k)
+                            if (j + u < nblk) x[u][k] = ldv<T, PV>(vr[k] + (int64_t)(j + u) * bstride);
+#pragma unroll
+                    for (int u = 0; u < UJ; ++u) {
+                        if (j + u < nblk) {
+#pragma unroll
+                            for (int q = 0; q < PV; ++q) {
+                                const T* yc = ys + (size_t)((j + u) * PV + q) * npad + o0;
+                                unsigned long long xx[RB];
+#pragma unroll
+                                for (int k = 0; k < RB; ++k) xx[k] = pack2(x[u][k].v[q], x[u][k].v[q]);
+#pragma unroll
+                                for (int o = 0; o < NO; o += 4) {
+                                    const Vec<T, 4> y = ldv<T, 4>(yc + o);
+                                    const unsigned long long y01 = pack2(y.v[0], y.v[1]);
+                                    const unsigned long long y23 = pack2(y.v[2], y.v[3]);
+#pragma unroll
+                                    for (int k = 0; k < RB; ++k) {
+                                        fma2(acc2[k][o / 2], xx[k], y01);
+                                        fma2(acc2[k][o / 2 + 1], xx[k], y23);
+                                    }
+                                }
+                            }
+                        }
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < RB; ++k)
+#pragma unroll
+                    for (int u = 0; u < NO / 2; ++u) {
+                        float lo, hi;
+                        unpack2(acc2[k][u], lo, hi);
+                        acc[k][2 * u] = lo;
+                        acc[k][2 * u + 1] = hi;
+                    }
+            } else if constexpr (PV >= 1) {
                 constexpr int UJ = PV == 1 ? 4 : 2;
                 for (int j = 0; j < nblk; j += UJ) {
                     Vec<T, PV> x[UJ][RB];
