@@ -12,12 +12,14 @@
 // dense block carved out of a 1000 x 1000 matrix.
 //
 // Here one thread owns one grid point.  h is symmetric tridiagonal and
-// generated on the fly from (mu, J, q, psi, p); its smallest eigenvalue comes
-// from Sturm-count bisection, bracketed by the Gershgorin lower bound and
-// min_i h_ii (and, for p > 1, by the previous truncation's energy: the
-// smallest eigenvalue cannot rise when a level is added), the ground vector
-// from two inverse-iteration sweeps, and the energy from its Rayleigh
-// quotient.  For psi = 0 or J = 0 h is diagonal; its ground vector is taken
+// generated on the fly from (mu, J, q, psi, p).  From 7 levels on its ground
+// state comes from Rayleigh-quotient iteration started at the previous
+// truncation's ground vector, certified by Sturm counts; the first
+// truncations (and any uncertified case) use Sturm-count bisection, bracketed
+// by the Gershgorin lower bound and min_i h_ii (and, for p > 1, by the
+// previous truncation's energy: the smallest eigenvalue cannot rise when a
+// level is added), the ground vector from two inverse-iteration sweeps, and
+// the energy from its Rayleigh quotient.  For psi = 0 or J = 0 h is diagonal; its ground vector is taken
 // as the unit vector of the first smallest diagonal entry, so psi = 0 is a
 // fixed point (the reference's Lanczos returns an arbitrary mixture when two
 // diagonal entries tie, at integer mu).
@@ -137,6 +139,60 @@ __device__ double mf_ground(int N, double mu, double c1, double c2, double hi_in
     return rq;
 }
 
+// Ground state by Rayleigh-quotient iteration from x (the previous
+// truncation's ground vector padded with zeros, an excellent start: adding
+// two levels barely moves it): at most four steps of x <- (h - rho I)^-1 x,
+// rho = x^T h x, then a certificate by two Sturm counts -- exactly one
+// eigenvalue below rho + delta and none below rho - delta.  Returns false
+// (x destroyed) when the certificate fails; the caller then bisects.
+__device__ bool mf_ground_rqi(int N, double mu, double c1, double c2, double* x, double* piv,
+                              const double* __restrict__ sq, double& e0) {
+    auto rayleigh = [&]() {
+        double r = 0.0;
+        for (int i = 0; i < N; ++i) {
+            r += mf_diag(i, mu, c2) * x[i] * x[i];
+            if (i + 1 < N) r += 2.0 * c1 * sq[i + 1] * x[i] * x[i + 1];
+        }
+        return r;
+    };
+    auto normalise = [&]() {
+        double nrm = 0.0;
+        for (int i = 0; i < N; ++i) nrm += x[i] * x[i];
+        if (!(nrm > 0.0) || !isfinite(nrm)) return false;
+        const double s = rsqrt(nrm);
+        for (int i = 0; i < N; ++i) x[i] *= s;
+        return true;
+    };
+    if (!normalise()) return false;
+    double rho = rayleigh();
+    const double tiny = 1e-15 * (fabs(rho) + fabs(c1) * sq[N] + 1.0);
+    for (int it = 0; it < 4; ++it) {
+        // (h - rho I) y = x in place, LDL^T without pivoting, |pivots| >= tiny
+        double p0 = mf_diag(0, mu, c2) - rho;
+        if (fabs(p0) < tiny) p0 = p0 < 0.0 ? -tiny : tiny;
+        piv[0] = 1.0 / p0;
+        for (int i = 1; i < N; ++i) {
+            const double e = c1 * sq[i];
+            double pi = mf_diag(i, mu, c2) - rho - e * e * piv[i - 1];
+            if (fabs(pi) < tiny) pi = pi < 0.0 ? -tiny : tiny;
+            piv[i] = 1.0 / pi;
+            x[i] -= e * piv[i - 1] * x[i - 1];
+        }
+        x[N - 1] *= piv[N - 1];
+        for (int i = N - 2; i >= 0; --i) x[i] = (x[i] - c1 * sq[i + 1] * x[i + 1]) * piv[i];
+        if (!normalise()) return false;
+        const double rn = rayleigh();
+        const bool done = fabs(rn - rho) <= 1e-15 * (fabs(rn) + 1.0);
+        rho = rn;
+        if (done) break;
+    }
+    const double delta = 1e-9 * (fabs(rho) + fabs(c1) + 1.0);
+    const double c1sq = c1 * c1;
+    if (mf_sturm(N, mu, c1sq, c2, rho + delta) != 1 || mf_sturm(N, mu, c1sq, c2, rho - delta) != 0) return false;
+    e0 = rho;
+    return true;
+}
+
 // Persistent threads: each thread takes the next grid point from *next
 // (points differ by orders of magnitude in their number of psi updates, so
 // static assignment would leave most lanes idle behind the slowest point).
@@ -167,8 +223,18 @@ k_scmf(int npts, const double* __restrict__ mu, const double* __restrict__ J, in
                     ok = false;
                     break;
                 }
-                // interlacing: the smallest eigenvalue cannot rise with p
-                const double e1 = mf_ground(2 * p + 1, m, c1, c2, e0 + 1e-12 * (fabs(e0) + 1.0), x, piv, sq);
+                // from 7 levels on: Rayleigh-quotient iteration from the previous
+                // ground vector; else (or if it cannot certify) bisection, whose
+                // bracket uses interlacing: the smallest eigenvalue cannot rise with p
+                const int N = 2 * p + 1;
+                double e1;
+                bool ok1 = false;
+                if (N >= 7 && c1 != 0.0) {
+                    x[N - 2] = 0.0;
+                    x[N - 1] = 0.0;
+                    ok1 = mf_ground_rqi(N, m, c1, c2, x, piv, sq, e1);
+                }
+                if (!ok1) e1 = mf_ground(N, m, c1, c2, e0 + 1e-12 * (fabs(e0) + 1.0), x, piv, sq);
                 tmp = fabs(e0 - e1);
                 e0 = e1;
             } while (tmp > eps);
