@@ -57,7 +57,7 @@ EXPORTS = [
     "bh_hamiltonian_create_matrix_free", "bh_hamiltonian_is_matrix_free",
     "bh_hamiltonian_destroy", "bh_hamiltonian_nnz", "bh_hamiltonian_csr",
     "bh_hamiltonian_apply", "bh_hamiltonian_apply_noalloc", "bh_solver_opts_default", "bh_eigsh", "bh_eigsh_csr",
-    "bh_eigsh_batch", "bh_eigsh_batch_sectors", "bh_dense_eigh", "bh_gap_ratios", "bh_spdm", "bh_phase_map", "bh_scmf", "bh_mean_field_grid", "bh_profile_enable",
+    "bh_eigsh_batch", "bh_eigsh_batch_vectors", "bh_eigsh_batch_sectors", "bh_dense_eigh", "bh_gap_ratios", "bh_spdm", "bh_phase_map", "bh_scmf", "bh_mean_field_grid", "bh_profile_enable",
     "bh_profile_reset", "bh_profile_count", "bh_profile_get",
 ]
 
@@ -103,6 +103,8 @@ def load() -> C.CDLL:
                                C.POINTER(bh_solve_info)]
     L.bh_eigsh_batch.argtypes = [vp, C.c_int, vp, vp, vp, C.POINTER(bh_solver_opts), vp, vp, vp,
                                  C.POINTER(bh_solve_info)]
+    L.bh_eigsh_batch_vectors.argtypes = [vp, C.c_int, vp, vp, vp, C.POINTER(bh_solver_opts), vp, vp, vp,
+                                         vp, C.POINTER(bh_solve_info)]
     L.bh_eigsh_batch_sectors.argtypes = [C.c_int, vp, C.c_int, vp, vp, vp, C.POINTER(bh_solver_opts), vp, vp, vp,
                                          C.POINTER(bh_solve_info)]
     L.bh_dense_eigh.argtypes = [C.c_int64, vp, vp, vp]
@@ -289,7 +291,10 @@ class Hamiltonian:
                                C.byref(info)))
         return ev, rs, (None if vec is None else vec.T.copy()), _info(info)
 
-    def eigsh_batch(self, J, U, mu, nev: int = 10, **opt):
+    def eigsh_batch(self, J, U, mu, nev: int = 10, vectors: bool = False, **opt):
+        """Batched lowest eigenpairs of (J[s], U[s], mu[s]).  Returns
+        ev, resid [S, nev], nconv [S], info, and with vectors=True also the
+        eigenvectors [S, nev, D] (rows in opt['order'], reference by default)."""
         J = np.ascontiguousarray(J, np.float64)
         S = len(J)
         U = np.ascontiguousarray(np.broadcast_to(U, (S,)), np.float64)
@@ -299,6 +304,11 @@ class Hamiltonian:
         rs = np.zeros((S, nev))
         nc = np.zeros(S, np.int32)
         info = bh_solve_info()
+        if vectors:
+            vec = np.zeros((S, nev, self.D))
+            _check(load().bh_eigsh_batch_vectors(self._h, S, _ptr(J), _ptr(U), _ptr(mu), C.byref(o),
+                                                 _ptr(ev), _ptr(rs), _ptr(nc), _ptr(vec), C.byref(info)))
+            return ev, rs, nc, _info(info), vec
         _check(load().bh_eigsh_batch(self._h, S, _ptr(J), _ptr(U), _ptr(mu), C.byref(o),
                                      _ptr(ev), _ptr(rs), _ptr(nc), C.byref(info)))
         return ev, rs, nc, _info(info)
@@ -482,6 +492,79 @@ class Analysis:
         _check(load().bh_phase_map(m, n_lo, nsec, nJ, _ptr(e0), len(mu), _ptr(mu), _ptr(dens),
                                    _ptr(kap)))
         return dens, kap
+
+    # ---- exact phase scan (analysis.cpp:207-427) ----
+    @staticmethod
+    def exact_parameters(m: int, n: int, J: float, U: float, mu: float, s: float, r: float,
+                         fixed_param: str, path: str | None = "phase.txt", nb_eigen: int = 20,
+                         precision: int = PREC_MIXED, max_batch: int = 128):
+        """Analysis::exact_parameters + calculate_and_save (analysis.cpp:207-427)
+        on the device: the 1D periodic chain of m sites with n bosons; one of
+        J, U, mu fixed ("J", "U", anything else = mu) and the other two swept
+        over [x, x + r] in steps s (the parameter pairing of analysis.cpp:245-257);
+        per grid point the lowest nb_eigen eigenvalues (batched solves), the
+        mean gap ratio, and the condensate fraction and coherence of the
+        single-particle density matrix of the eigenvector whose eigenvalue has
+        the largest magnitude (the reference's first IRLM_eigen column).  The
+        nb_eigen += 5 loop repeats while the gap-ratio variance stays at or below
+        1e-8 of its mean (analysis.cpp:362-379).  Writes phase.txt like
+        analysis.cpp:269-274, 384-387 when path is given.  Returns
+        (param1, param2, gap_ratio, condensate_fraction, coherence) arrays."""
+        import sys as _sys
+
+        eps = np.finfo(float).eps
+        if abs(J) < eps and abs(U) < eps and abs(mu) < eps:
+            print("Error: At least one of the parameters J, U, mu must be different from zero.",
+                  file=_sys.stderr)
+            return None
+        nb = Neighbours(m)
+        nb.chain_neighbours()
+        h = Hamiltonian(Basis(m, n), nb.getNeighbours())
+        if fixed_param == "J":
+            fixed_value, r1, r2 = J, (J, J + r), (mu, mu + r)
+            point = lambda p1, p2: (J, p1, p2)  # noqa: E731  (H_fixed = J T, H1 = V, H2 = -N)
+        elif fixed_param == "U":
+            fixed_value, r1, r2 = U, (J, J + r), (U, U + r)
+            point = lambda p1, p2: (p1, U, p2)  # noqa: E731  (H_fixed = U V, H1 = T, H2 = -N)
+        else:
+            fixed_value, r1, r2 = mu, (J, J + r), (mu, mu + r)
+            point = lambda p1, p2: (p1, p2, mu)  # noqa: E731  (H_fixed = -mu N, H1 = T, H2 = V)
+        n1 = int((r1[1] - r1[0]) / s) + 1
+        n2 = int((r2[1] - r2[0]) / s) + 1
+        P1 = np.zeros(n1 * n2)
+        P2 = np.zeros(n1 * n2)
+        for i in range(n1):  # row-major over (param1, param2); the reference indexes
+            for j in range(n2):  # i * num_param1 + j, which equals this when n1 == n2
+                P1[i * n2 + j] = r1[0] + i * s
+                P2[i * n2 + j] = r2[0] + j * s
+        pts = np.array([point(a, b) for a, b in zip(P1, P2)])
+        while True:
+            gap = np.zeros(len(P1))
+            cf = np.zeros(len(P1))
+            coh = np.zeros(len(P1))
+            for k0 in range(0, len(P1), max_batch):
+                sl = slice(k0, min(len(P1), k0 + max_batch))
+                ev, _, nc, _, vec = h.eigsh_batch(pts[sl, 0], pts[sl, 1], pts[sl, 2], nev=nb_eigen,
+                                                  vectors=True, precision=precision)
+                for k in range(ev.shape[0]):
+                    ratios = Analysis.gap_ratios(ev[k], nb_eigen)
+                    gap[k0 + k] = ratios.sum() / len(ratios) if len(ratios) else 0.0
+                    phi = vec[k, int(np.argmax(np.abs(ev[k])))]
+                    rho = h.spdm(phi)
+                    w = np.linalg.eigvalsh(rho)
+                    cf[k0 + k] = abs(w[int(np.argmax(np.abs(w)))] / np.trace(rho))
+                    coh[k0 + k] = Analysis.coherence(rho)
+            mean = gap.mean()
+            var = np.mean((gap - mean) ** 2)
+            if var > 1e-8 * mean or nb_eigen + 5 > h.D:
+                break
+            nb_eigen += 5
+        if path:
+            with open(path, "w") as f:
+                f.write(f"{fixed_param} {fixed_value:g}\n")
+                for k in range(len(P1)):
+                    f.write(f"{P1[k]:g} {P2[k]:g} {gap[k]:g} {cf[k]:g} {coh[k]:g}\n")
+        return P1, P2, gap, cf, coh
 
     # ---- mean field (analysis.cpp:58-178) ----
     @staticmethod

@@ -375,6 +375,32 @@ int bh_eigsh_batch(const bh_hamiltonian* h, int nsolve, const double* J, const d
     });
 }
 
+int bh_eigsh_batch_vectors(const bh_hamiltonian* h, int nsolve, const double* J, const double* U,
+                           const double* mu, const bh_solver_opts* o, double* evals, double* resid,
+                           int* nconv, double* evecs, bh_solve_info* info) {
+    return guard([&] {
+        const auto t0 = std::chrono::steady_clock::now();
+        BH_REQUIRE(h != nullptr && J && U && mu && evals && evecs, "null argument");
+        BH_REQUIRE(nsolve >= 1, "nsolve must be >= 1");
+        check_solver_opts(o);
+        SolveRequest rq = make_request(o, h->D, nsolve);
+        rq.want_vectors = true;
+        rq.d_perm = h->basis->d_col_of_lex.p;
+        rq.J.assign(J, J + nsolve);
+        rq.U.assign(U, U + nsolve);
+        rq.shift.resize(nsolve);
+        for (int s = 0; s < nsolve; ++s) rq.shift[s] = -mu[s] * (double)h->n;
+        Stream st;
+        SolveResult r = block_lanczos(op64_of(h), op32_of(h), rq, st);
+        std::memcpy(evals, r.evals.data(), r.evals.size() * sizeof(double));
+        if (resid) std::memcpy(resid, r.resid.data(), r.resid.size() * sizeof(double));
+        if (nconv) std::memcpy(nconv, r.nconv.data(), nsolve * sizeof(int));
+        write_vectors(h, r, nsolve, o->nev, o->order, evecs);
+        const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        fill_info(info, r, o->nev, secs);
+    });
+}
+
 int bh_eigsh_batch_sectors(int nh, const bh_hamiltonian* const* hs, int nsolve, const double* J,
                            const double* U, const double* mu, const bh_solver_opts* o, double* evals,
                            double* resid, int* nconv, bh_solve_info* info) {

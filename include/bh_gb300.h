@@ -196,6 +196,12 @@ int bh_eigsh_csr(int64_t dim, const int64_t* row_ptr, const int32_t* col, const 
 int bh_eigsh_batch(const bh_hamiltonian* h, int nsolve, const double* J, const double* U,
                    const double* mu, const bh_solver_opts* o, double* evals, double* resid,
                    int* nconv, bh_solve_info* info);
+/* bh_eigsh_batch with the eigenvectors: evecs[(s*nev + i)*D + r] (host,
+ * D*nev doubles per solve, rows in o->order), the i-th lowest eigenvector of
+ * solve s (FP64 Rayleigh-Ritz vectors of either precision). */
+int bh_eigsh_batch_vectors(const bh_hamiltonian* h, int nsolve, const double* J, const double* U,
+                           const double* mu, const bh_solver_opts* o, double* evals, double* resid,
+                           int* nconv, double* evecs, bh_solve_info* info);
 /* The same batch over nh Hamiltonians (the particle-number sectors of a
  * phase diagram, of uneven dimension) in one call: the sectors run
  * concurrently on the device, each on its own stream driven by its own host
