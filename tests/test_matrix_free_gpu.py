@@ -97,3 +97,20 @@ def test_matrix_free_rejects_wide_strings(pkg):
     b = pkg.Basis(17, 8)
     with pytest.raises(ValueError, match="64 bits"):
         pkg.Hamiltonian(b, chain_lists(17), matrix_free=True)
+
+
+def test_matrix_free_wide_batch_block4(pkg):
+    # 16 solves x block 4 = 64 columns: the 32-lane matrix-free kernel and the
+    # fused (block 4) CSR epilogue, both precisions, against each other
+    m, n = 16, 6  # 4x4 torus, D = 54264
+    lists = square_lists(pkg, m)
+    b = pkg.Basis(m, n)
+    hc = pkg.Hamiltonian(b, lists)
+    hf = pkg.Hamiltonian(b, lists, matrix_free=True)
+    Js = np.linspace(0.02, 0.1, 16)
+    ev_c, _, nc_c, _ = hc.eigsh_batch(Js, 1.0, 0.4, nev=4, block=4, precision=pkg.PREC_FP64)
+    ev_f, _, nc_f, _ = hf.eigsh_batch(Js, 1.0, 0.4, nev=4, block=4, precision=pkg.PREC_MIXED, ncv=60)
+    ev_cm, _, nc_cm, _ = hc.eigsh_batch(Js, 1.0, 0.4, nev=4, block=4, precision=pkg.PREC_MIXED, ncv=60)
+    assert min(nc_c.min(), nc_f.min(), nc_cm.min()) >= 4
+    np.testing.assert_allclose(ev_f, ev_c, rtol=1e-8, atol=1e-10)
+    np.testing.assert_allclose(ev_cm, ev_c, rtol=1e-8, atol=1e-10)
