@@ -2,10 +2,10 @@
  * bh_oracle.c -- CPU ORACLE for the Bose-Hubbard exact-diagonalisation path.
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product (the CUDA library and its
- * host mirror) links, loads or calls this file.  It is used by tests/ as the
- * checker, by __graft_entry__.smoke() as the checker, and by bench.py's CPU
- * baseline leg / reference arm as the timed CPU restatement ("port") of the
- * reference's exact path.
+ * host mirror) links, loads or calls this file.  tests/ and
+ * __graft_entry__.smoke() compare the device results with it, and bench.py's
+ * CPU baseline leg / reference arm times it as the CPU restatement ("port")
+ * of the reference's exact path.
  *
  * It restates, in plain C, the reference's algorithms for this path
  * (Maximilien-Hantonne/Bose-Hubbard-Phase-Transition):

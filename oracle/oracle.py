@@ -1,8 +1,9 @@
 """ctypes front-end of the CPU oracle (TEST INFRASTRUCTURE ONLY).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference
-arm may import this module, and only as the checker or as the timed CPU
-restatement of the reference's path; the product library never does.
+arm may import this module, and only to check results against the oracle or
+as the timed CPU restatement of the reference's path; the product library
+never does.
 
 `Oracle` wraps oracle/liboracle.so (plain-C restatement of the reference's
 basis, Hamiltonian, IRLM eigensolver and observables, see bh_oracle.c for the
