@@ -1201,7 +1201,8 @@ struct Launcher {
     int64_t* launches;
 
     void done(const char* name, double bytes) const {
-        BH_CUDA(cudaGetLastError());
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) throw Error(BH_ERR_CUDA, std::string("launch of ") + name + ": " + cudaGetErrorString(e));
         ++*launches;
         profile_end(st, name, bytes);
     }
@@ -1220,7 +1221,7 @@ struct Launcher {
         dim3 grid(g.nchunks, (nblk + JT - 1) / JT);
         const size_t smem = (size_t)g.NT * JT * PMAX * sizeof(double);
         auto kern = k_dot<T, PMAX, JT>;
-        if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        allow_large_smem(kern, smem);
         profile_begin(st);
         kern<<<grid, g.NT, smem, st>>>(op.D, g.ncols, ld, p, nblk, bstride, V, W, g.rows_per_chunk, kcap, part);
         done(nblk == 1 ? "k_dot(1 block)" : "k_dot", (double)(nblk + 1) * op.D * g.ncols * sizeof(T));
@@ -1240,7 +1241,7 @@ struct Launcher {
         dim3 grid((nblk + JT - 1) / JT, g.nchunks);
         const size_t smem = (size_t)NT * JT * P * P * sizeof(double);
         auto kern = k_dotv<T, P, JT, RU>;
-        if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        allow_large_smem(kern, smem);
         profile_begin(st);
         kern<<<grid, NT, smem, st>>>(op.D, S, nblk, bstride, V, W, g.rows_per_chunk, kcap, part);
         done(nblk == 1 ? "k_dot(1 block)" : "k_dot", (double)(nblk + 1) * op.D * g.ncols * sizeof(T));
@@ -1291,7 +1292,7 @@ struct Launcher {
                             (size_t)g.NT * PMAX * sizeof(double);
         if ((int)smem > max_smem_optin()) throw Error(BH_ERR_ARG, "Krylov basis too wide for shared memory (reduce ncv or batch)");
         auto kern = k_update<T, PMAX>;
-        if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        allow_large_smem(kern, smem);
         profile_begin(st);
         kern<<<g.nchunks, g.NT, smem, st>>>(op.D, g.ncols, p, ilog2(p), kc, bstride, V, Cf, W,
                                             g.rows_per_chunk, do_gram, gpart);
@@ -1307,7 +1308,7 @@ struct Launcher {
                             (size_t)NT * P * P * sizeof(double);
         if ((int)smem > max_smem_optin()) throw Error(BH_ERR_ARG, "Krylov basis too wide for shared memory (reduce ncv or batch)");
         auto kern = k_updatev<T, P>;
-        if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        allow_large_smem(kern, smem);
         profile_begin(st);
         kern<<<g.nchunks, NT, smem, st>>>(op.D, S, kc / P, bstride, V, Cf, W, g.rows_per_chunk, do_gram, gpart);
         done(name ? name : (kc > 0 ? "k_update" : "k_update(gram)"),
@@ -1342,7 +1343,7 @@ struct Launcher {
         const int NT = S * std::max(1, 256 / S);
         const size_t smem = do_gram ? (size_t)NT * P * P * sizeof(double) : 0;
         auto kern = k_normgram<T, P>;
-        if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        allow_large_smem(kern, smem);
         profile_begin(st);
         kern<<<g.nchunks, NT, smem, st>>>(op.D, S, nR, Rinv, rstride, W, Vout, g.rows_per_chunk, do_gram, gpart,
                                           skip_if_zero, reset);
@@ -1392,7 +1393,7 @@ struct Launcher {
         const bool vec = (p == 1 || p == 2 || p == 4) && ld_in % p == 0 && bstride % p == 0 &&
                          ((uintptr_t)V % ((uintptr_t)p * sizeof(T))) == 0;
         auto launch = [&](auto kern) {
-            if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            allow_large_smem(kern, smem);
             kern<<<dim3((unsigned)ngroups, (unsigned)chunks), 128, smem, st>>>(
                 op.D, Sproc, ld_in, p, kc, nout, bstride, V, Yg, in_idx, out_idx, Vout, ostride,
                 ld_out, single, Sg, npad, ystride, rpc);
@@ -1595,6 +1596,7 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
             if (exec) cudaGraphExecDestroy(exec);
         }
     } cgs[2];
+    bool graphs_failed = false;
     auto run_steps = [&](int ncols, int64_t bstride, const Geo& g, const Geo& gu) {
         for (int j = jstart; j < nb; ++j) {
             T* Vj = Va.p + (int64_t)j * bstride;
@@ -1626,7 +1628,7 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
         const int ncols = S * p;
         const int64_t bstride = D * ncols;
         const Geo g = make_geo(D, ncols), gu = make_ugeo(D, ncols);
-        const bool graphs = after_restart && use_graphs() && !profile_on() && !debug_ortho();
+        const bool graphs = after_restart && !graphs_failed && use_graphs() && !profile_on() && !debug_ortho();
         CycleGraph& cg = cgs[restarts & 1];
         if (graphs && cg.exec && cg.S == S && cg.jstart == jstart && cg.after == after_restart &&
             cg.va == Va.p) {
@@ -1652,7 +1654,19 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
             cudaGraphExec_t exec = nullptr;
             const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
             cudaGraphDestroy(graph);
-            BH_CUDA(e);
+            if (e != cudaSuccess) {
+                // nothing of the captured cycle has run: launch it directly
+                // and keep direct launches for the rest of this solve
+                (void)cudaGetLastError();
+                if (verbose())
+                    std::fprintf(stderr, "[bh] cycle graph not instantiated (%s): direct launches\n",
+                                 cudaGetErrorString(e));
+                graphs_failed = true;
+                res.launches = l0;
+                res.matvecs = m0;
+                run_steps(ncols, bstride, g, gu);
+                goto cycle_done;
+            }
             cg.exec = exec;
             cg.S = S;
             cg.jstart = jstart;
@@ -1664,6 +1678,7 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
         } else {
             run_steps(ncols, bstride, g, gu);
         }
+    cycle_done:
         if (debug_ortho()) {
             // Gram matrix of all nb + 1 blocks against each block, solve 0
             double worst = 0.0;

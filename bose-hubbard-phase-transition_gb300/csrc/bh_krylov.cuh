@@ -24,6 +24,21 @@ struct OpView {
     int m = 0, n = 0, bits = 0, nbonds = 0;
 };
 
+// Lets kern take more than 48 KB of dynamic shared memory.  The attribute is
+// per function and process-wide, and solves of other sectors set it from
+// other host threads: it is therefore only ever set to the device's opt-in
+// maximum (never to a launch's own size, which another thread could lower
+// between this thread's setting and its launch).
+template <class K>
+inline void allow_large_smem(K kern, size_t smem) {
+    if (smem <= 48 * 1024) return;
+    int dev = 0, mx = 0;
+    BH_CUDA(cudaGetDevice(&dev));
+    BH_CUDA(cudaDeviceGetAttribute(&mx, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    BH_REQUIRE(smem <= (size_t)mx, "shared memory of a launch exceeds the device limit");
+    BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+}
+
 // Operator views of a built Hamiltonian (CSR or matrix-free).
 template <class T>
 inline OpView<T> op_view(const bh_hamiltonian* h) {

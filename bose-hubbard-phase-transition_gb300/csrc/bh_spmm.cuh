@@ -319,7 +319,7 @@ double launch_spmm_kind(const OpView<T>& op, int ncols, int group, const double*
         constexpr int LL = decltype(lc)::value, CC = decltype(cwc)::value;
         if constexpr (MF) {
             auto kern = k_spmm_mf<T, LL, CC>;
-            if (smem > 48 * 1024) BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            allow_large_smem(kern, smem);
             kern<<<(unsigned)g, 256, smem, st>>>(op, ncols, group, prm, X, Y);
         }
         else if (fuse && group == 2)

@@ -153,7 +153,7 @@ int bh_hamiltonian_apply_noalloc(const bh_hamiltonian* h, int order, double J, d
 
 typedef struct bh_solver_opts {
     int nev;          /* wanted lowest eigenvalues (the reference's nb_eigen)         */
-    int ncv;          /* max Krylov basis size per solve; 0 = automatic               */
+    int ncv;          /* max Krylov basis size per solve; 0 = max(7 nev, nev + 8 block) */
     int block;        /* block size p (>= degeneracy to resolve); 0 = automatic       */
     int precision;    /* BH_PREC_FP64 or BH_PREC_MIXED                                 */
     int max_restarts; /* restart cap (the reference's maxit = 1000)                    */
