@@ -865,13 +865,38 @@ k_rotate(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t bstri
 #pragma unroll
                     for (int u = 0; u < NO / 2; ++u) acc2[k][u] = 0ull;
                 constexpr int UJ = PV == 1 ? 4 : 2;
-                for (int j = 0; j < nblk; j += UJ) {
-                    Vec<T, PV> x[UJ][RB];
+                // PF: the next UJ blocks' values are requested before this
+                // group's products (one group of loads always in flight), where
+                // the extra registers keep three CTAs per SM
+                constexpr bool PF = PV * UJ * RB <= 8;
+                Vec<T, PV> xn[PF ? UJ : 1][RB];
+                if constexpr (PF) {
 #pragma unroll
                     for (int u = 0; u < UJ; ++u)
 #pragma unroll
                         for (int k = 0; k < RB; ++k)
-                            if (j + u < nblk) x[u][k] = ldv<T, PV>(vr[k] + (int64_t)(j + u) * bstride);
+                            if (u < nblk) xn[u][k] = ldv<T, PV>(vr[k] + (int64_t)u * bstride);
+                }
+                for (int j = 0; j < nblk; j += UJ) {
+                    Vec<T, PV> x[UJ][RB];
+                    if constexpr (PF) {
+#pragma unroll
+                        for (int u = 0; u < UJ; ++u)
+#pragma unroll
+                            for (int k = 0; k < RB; ++k) x[u][k] = xn[u][k];
+#pragma unroll
+                        for (int u = 0; u < UJ; ++u)
+#pragma unroll
+                            for (int k = 0; k < RB; ++k)
+                                if (j + UJ + u < nblk)
+                                    xn[u][k] = ldv<T, PV>(vr[k] + (int64_t)(j + UJ + u) * bstride);
+                    } else {
+#pragma unroll
+                        for (int u = 0; u < UJ; ++u)
+#pragma unroll
+                            for (int k = 0; k < RB; ++k)
+                                if (j + u < nblk) x[u][k] = ldv<T, PV>(vr[k] + (int64_t)(j + u) * bstride);
+                    }
 #pragma unroll
                     for (int u = 0; u < UJ; ++u) {
                         if (j + u < nblk) {

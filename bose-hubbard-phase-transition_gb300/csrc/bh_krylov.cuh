@@ -39,6 +39,14 @@ inline void allow_large_smem(K kern, size_t smem) {
     BH_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
 }
 
+// CTAs of kern resident on one SM at this block size and dynamic shared memory.
+template <class K>
+inline int resident_ctas(K kern, int threads, size_t smem) {
+    int n = 0;
+    BH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, threads, smem));
+    return n;
+}
+
 // Operator views of a built Hamiltonian (CSR or matrix-free).
 template <class T>
 inline OpView<T> op_view(const bh_hamiltonian* h) {

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <type_traits>
 
@@ -280,6 +281,18 @@ k_spmm_mf(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
     }
 }
 
+// Resident CTAs per SM of the fused CSR product (found once per instance).
+template <class T, int L, int CW, int DP>
+int spmm_fused_per_sm() {
+    static std::atomic<int> occ{0};
+    int n = occ.load(std::memory_order_relaxed);
+    if (n == 0) {
+        n = std::max(1, resident_ctas(k_spmm<T, L, CW, DP>, 256, (size_t)256 * CW * DP * sizeof(double)));
+        occ.store(n, std::memory_order_relaxed);
+    }
+    return n;
+}
+
 // Launch of Y = H X on a CSR (MF = false) or matrix-free (MF = true)
 // operator: L lanes per row over the columns (the largest power of two <= 32
 // dividing ncols), CW columns per lane per pass (1 or 2 when that covers the
@@ -300,10 +313,6 @@ double launch_spmm_kind(const OpView<T>& op, int ncols, int group, const double*
     // fused X^T Y partials: CSR, one pass over the columns, block size 2 or 4
     const bool fuse = !MF && dpart && (group == 2 || group == 4) && cpl <= CW && L >= group;
     if (dparts) *dparts = 0;
-    if (fuse) {
-        g = std::min<int64_t>(g, (int64_t)sm_count() * 4);  // fewer partial rows to reduce
-        if (dparts) *dparts = (int)g;
-    }
     size_t smem = 0;
     if (MF) {
         BH_REQUIRE(op.nbonds <= 128, "matrix-free product: at most 128 directed bonds");
@@ -322,11 +331,21 @@ double launch_spmm_kind(const OpView<T>& op, int ncols, int group, const double*
             allow_large_smem(kern, smem);
             kern<<<(unsigned)g, 256, smem, st>>>(op, ncols, group, prm, X, Y);
         }
-        else if (fuse && group == 2)
-            k_spmm<T, LL, CC, 2><<<(unsigned)g, 256, 256 * CC * 2 * sizeof(double), st>>>(op, ncols, group, prm, X, Y, dpart);
-        else if (fuse && group == 4)
-            k_spmm<T, LL, CC, 4><<<(unsigned)g, 256, 256 * CC * 4 * sizeof(double), st>>>(op, ncols, group, prm, X, Y, dpart);
-        else k_spmm<T, LL, CC, 0><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y, nullptr);
+        else if (fuse) {
+            // one resident wave (fewer partial rows to reduce, no tail wave)
+            auto fused = [&](auto dpc) {
+                constexpr int DPP = decltype(dpc)::value;
+                const int per_sm = std::min(4, spmm_fused_per_sm<T, LL, CC, DPP>());
+                const int64_t gf = std::min<int64_t>(g, (int64_t)sm_count() * per_sm);
+                if (dparts) *dparts = (int)gf;
+                k_spmm<T, LL, CC, DPP><<<(unsigned)gf, 256, 256 * CC * DPP * sizeof(double), st>>>(
+                    op, ncols, group, prm, X, Y, dpart);
+            };
+            if (group == 2) fused(std::integral_constant<int, 2>());
+            else fused(std::integral_constant<int, 4>());
+        } else {
+            k_spmm<T, LL, CC, 0><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y, nullptr);
+        }
     };
     auto odd_share = [&](auto lc) {
         if (CW == 1) go(lc, std::integral_constant<int, 1>());
