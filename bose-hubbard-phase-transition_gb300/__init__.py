@@ -346,6 +346,72 @@ def _info(i: bh_solve_info) -> SolveInfo:
 
 
 # ---------------------------------------------------------------------------
+# the grid over several ranks (one process per GPU): the (J, sector) points
+# are independent eigensolves, so ranks split the J points and solve their
+# share with no exchange; only the eigenvalues are gathered at the end
+# ---------------------------------------------------------------------------
+def shard_indices(n_points: int, world: int, rank: int) -> np.ndarray:
+    """Grid points of `rank`: rank, rank + world, rank + 2 world, ...  The
+    shares are disjoint, cover 0..n_points-1, differ in size by at most one,
+    and each spans the whole J range (similar solve cost on every rank)."""
+    if world < 1 or not 0 <= rank < world or n_points < 0:
+        raise ValueError("need world >= 1, 0 <= rank < world and n_points >= 0")
+    return np.arange(rank, n_points, world, dtype=np.int64)
+
+
+def gather_grid(local: np.ndarray, n_points: int, group=None) -> np.ndarray:
+    """Full grid from every rank's share: `local` holds this rank's rows
+    (points shard_indices(n_points, world, rank), in that order, along axis 0
+    of shape [k, ...]); returns the [n_points, ...] array on every rank.
+    Host arrays through torch.distributed.all_gather_object (gloo or NCCL):
+    the results, not the data path, cross ranks."""
+    import torch.distributed as dist
+
+    local = np.asarray(local)
+    if not (dist.is_available() and dist.is_initialized()):
+        if local.shape[0] != n_points:
+            raise ValueError("without a process group the share is the whole grid")
+        return local.copy()
+    world = dist.get_world_size(group)
+    rank = dist.get_rank(group)
+    mine = shard_indices(n_points, world, rank)
+    if local.shape[0] != len(mine):
+        raise ValueError(f"rank {rank} holds {local.shape[0]} points, its share is {len(mine)}")
+    parts = [None] * world
+    dist.all_gather_object(parts, local, group=group)
+    out = np.empty((n_points,) + local.shape[1:], dtype=local.dtype)
+    for r, part in enumerate(parts):
+        out[shard_indices(n_points, world, r)] = part
+    return out
+
+
+def eigsh_sectors_sharded(hams, J, U, mu, nev: int = 10, group=None, **opt):
+    """eigsh_sectors over the ranks of a torch.distributed process group:
+    this rank solves its share of the J points (shard_indices) in every
+    sector, then the eigenvalues and convergence counts are gathered so that
+    every rank returns the whole grid: ev [nh, S, nev], nconv [nh, S], and
+    this rank's SolveInfo."""
+    import torch.distributed as dist
+
+    J = np.ascontiguousarray(J, np.float64)
+    S = len(J)
+    U = np.broadcast_to(np.asarray(U, np.float64), (S,))
+    mu = np.broadcast_to(np.asarray(mu, np.float64), (S,))
+    on = dist.is_available() and dist.is_initialized()
+    world = dist.get_world_size(group) if on else 1
+    rank = dist.get_rank(group) if on else 0
+    mine = shard_indices(S, world, rank)
+    nh = len(hams)
+    if len(mine):
+        ev, _, nc, info = eigsh_sectors(hams, J[mine], U[mine], mu[mine], nev=nev, **opt)
+    else:
+        ev, nc, info = np.zeros((nh, 0, nev)), np.zeros((nh, 0), np.int32), None
+    ev_all = gather_grid(np.moveaxis(ev, 1, 0), S, group)    # [S, nh, nev]
+    nc_all = gather_grid(np.moveaxis(nc, 1, 0), S, group)    # [S, nh]
+    return np.moveaxis(ev_all, 0, 1), np.moveaxis(nc_all, 0, 1), info
+
+
+# ---------------------------------------------------------------------------
 # tracing: per-kernel device time (CUDA events) and algorithmic bytes
 # ---------------------------------------------------------------------------
 def profile_enable(on: bool = True):
