@@ -50,6 +50,18 @@ class bh_solve_info(C.Structure):
     ]
 
 
+class bh_spmm_shape(C.Structure):
+    _fields_ = [("lanes", C.c_int), ("cols_per_lane", C.c_int), ("grid", C.c_int64)]
+
+
+class bh_spmm_tuning(C.Structure):
+    _fields_ = [
+        ("matrix_free", C.c_int), ("elem_bytes", C.c_int), ("dim", C.c_int64), ("nnz", C.c_int64),
+        ("ncols", C.c_int), ("shape", bh_spmm_shape), ("ms", C.c_float), ("ms_default", C.c_float),
+        ("candidates", C.c_int),
+    ]
+
+
 EXPORTS = [
     "bh_last_error", "bh_version", "bh_neighbours_chain", "bh_neighbours_square",
     "bh_neighbours_cube", "bh_dimension", "bh_basis_create", "bh_basis_destroy",
@@ -59,6 +71,8 @@ EXPORTS = [
     "bh_hamiltonian_apply", "bh_hamiltonian_apply_noalloc", "bh_solver_opts_default", "bh_eigsh", "bh_eigsh_csr",
     "bh_eigsh_batch", "bh_eigsh_batch_vectors", "bh_eigsh_batch_sectors", "bh_dense_eigh", "bh_gap_ratios", "bh_spdm", "bh_phase_map", "bh_scmf", "bh_mean_field_grid", "bh_profile_enable",
     "bh_profile_reset", "bh_profile_count", "bh_profile_get",
+    "bh_spmm_candidates", "bh_hamiltonian_apply_shape", "bh_spmm_autotune", "bh_spmm_tuning_count",
+    "bh_spmm_tuning_get", "bh_spmm_tuning_reset",
 ]
 
 _lib = None
@@ -117,6 +131,13 @@ def load() -> C.CDLL:
     L.bh_profile_enable.argtypes = [C.c_int]
     L.bh_profile_count.argtypes = [C.POINTER(C.c_int)]
     L.bh_profile_get.argtypes = [C.c_int, C.c_char_p, C.c_int, i64p, f64p, f64p]
+    L.bh_spmm_candidates.argtypes = [C.c_int, C.POINTER(bh_spmm_shape), C.c_int, C.POINTER(C.c_int)]
+    L.bh_hamiltonian_apply_shape.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
+                                             C.POINTER(bh_spmm_shape), vp, vp]
+    L.bh_spmm_autotune.argtypes = [vp, C.c_int, C.c_int, C.POINTER(bh_spmm_shape),
+                                   C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    L.bh_spmm_tuning_count.argtypes = [C.POINTER(C.c_int)]
+    L.bh_spmm_tuning_get.argtypes = [C.c_int, C.POINTER(bh_spmm_tuning)]
     _lib = L
     return L
 
@@ -280,6 +301,26 @@ class Hamiltonian:
         _check(load().bh_hamiltonian_apply(self._h, order, J, U, mu, X.shape[1], _ptr(X), _ptr(Y)))
         return Y.reshape(x.shape)
 
+    def apply_shape(self, x: np.ndarray, J: float, U: float, mu: float, shape=None,
+                    precision: int = PREC_FP64):
+        """y = H x in the lexicographic order with a given launch shape of the
+        product ((lanes, cols_per_lane, grid) or None for the default); FP64,
+        or FP32 vectors and values with PREC_MIXED."""
+        x = np.asarray(x, np.float64)
+        X = np.ascontiguousarray(x.reshape(self.D, -1))
+        Y = np.zeros_like(X)
+        sh = None if shape is None else C.byref(bh_spmm_shape(*shape))
+        _check(load().bh_hamiltonian_apply_shape(self._h, precision, J, U, mu, X.shape[1], sh,
+                                                 _ptr(X), _ptr(Y)))
+        return Y.reshape(x.shape)
+
+    def autotune(self, nvec: int, precision: int = PREC_MIXED) -> dict:
+        """Times the product's launch shapes for nvec columns now and records
+        the fastest for this operator's width class."""
+        sh, ms, md = bh_spmm_shape(), C.c_float(), C.c_float()
+        _check(load().bh_spmm_autotune(self._h, nvec, precision, C.byref(sh), C.byref(ms), C.byref(md)))
+        return {"shape": (sh.lanes, sh.cols_per_lane, sh.grid), "ms": ms.value, "ms_default": md.value}
+
     def eigsh(self, J: float, U: float, mu: float, nev: int = 10, vectors: bool = False,
               order: int = ORDER_REFERENCE, **opt):
         o = default_opts(nev=nev, order=order, **opt)
@@ -434,6 +475,38 @@ def profile_read() -> dict:
         _check(L.bh_profile_get(i, name, 64, C.byref(k), C.byref(ms), C.byref(by)))
         out[name.value.decode()] = {"launches": k.value, "ms": ms.value, "bytes": by.value}
     return out
+
+
+# ---------------------------------------------------------------------------
+# launch shapes of the sparse product and the autotuner's table
+# ---------------------------------------------------------------------------
+def spmm_candidates(nvec: int) -> list[tuple[int, int, int]]:
+    """(lanes, cols_per_lane, grid) shapes the tuner times for nvec columns,
+    the default first (grid 0: default, -1: one resident wave)."""
+    buf = (bh_spmm_shape * 32)()
+    n = C.c_int()
+    _check(load().bh_spmm_candidates(nvec, buf, 32, C.byref(n)))
+    return [(buf[i].lanes, buf[i].cols_per_lane, buf[i].grid) for i in range(n.value)]
+
+
+def spmm_tuning_table() -> list[dict]:
+    """Entries of the process-wide tuning table."""
+    L = load()
+    n = C.c_int()
+    _check(L.bh_spmm_tuning_count(C.byref(n)))
+    out = []
+    for i in range(n.value):
+        e = bh_spmm_tuning()
+        _check(L.bh_spmm_tuning_get(i, C.byref(e)))
+        out.append({"matrix_free": bool(e.matrix_free), "elem_bytes": e.elem_bytes, "dim": e.dim,
+                    "nnz": e.nnz, "ncols": e.ncols,
+                    "shape": (e.shape.lanes, e.shape.cols_per_lane, e.shape.grid),
+                    "ms": e.ms, "ms_default": e.ms_default, "candidates": e.candidates})
+    return out
+
+
+def spmm_tuning_reset():
+    _check(load().bh_spmm_tuning_reset())
 
 
 # ---------------------------------------------------------------------------

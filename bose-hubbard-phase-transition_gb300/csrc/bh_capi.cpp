@@ -610,7 +610,123 @@ int bh_phase_map(int m, int n_lo, int nsec, int nJ, const double* e0, int nmu, c
     });
 }
 
+// ---- launch shapes of the sparse product and the autotuner ----
+static SpmmShape shape_in(const bh_spmm_shape& s) {
+    SpmmShape o;
+    o.L = s.lanes;
+    o.CW = s.cols_per_lane;
+    o.grid = s.grid;
+    return o;
+}
+
+static bh_spmm_shape shape_out(const SpmmShape& s) {
+    bh_spmm_shape o;
+    o.lanes = s.L;
+    o.cols_per_lane = s.CW;
+    o.grid = s.grid;
+    return o;
+}
+
+int bh_spmm_candidates(int nvec, bh_spmm_shape* out, int cap, int* count) {
+    return guard([&] {
+        BH_REQUIRE(nvec >= 1 && count, "null argument or nvec < 1");
+        const std::vector<SpmmChoice> c = spmm_candidates(nvec);
+        BH_REQUIRE(cap >= (int)c.size() && out, "output capacity too small");
+        for (size_t i = 0; i < c.size(); ++i) out[i] = shape_out(spmm_resolve(c[i], nvec));
+        *count = (int)c.size();
+    });
+}
+
+int bh_hamiltonian_apply_shape(const bh_hamiltonian* h, int precision, double J, double U,
+                               double mu, int nvec, const bh_spmm_shape* shape, const double* x,
+                               double* y) {
+    return guard([&] {
+        BH_REQUIRE(h != nullptr && x && y && nvec >= 1, "null argument");
+        BH_REQUIRE(precision == BH_PREC_FP64 || precision == BH_PREC_MIXED, "unknown precision mode");
+        const SpmmShape s = shape ? shape_in(*shape) : spmm_resolve(SpmmChoice{}, nvec);
+        BH_REQUIRE(spmm_shape_valid(s, nvec),
+                   "launch shape: lanes must be a power of two <= 32 dividing nvec, columns per "
+                   "lane 1 or 4 (or 2 with 32 lanes), grid >= -1");
+        const int64_t D = h->D, n = D * nvec;
+        Stream st;
+        DevBuf<double> dx(n), dy(n), prm(3);
+        const double hp[3] = {J, U, -mu * (double)h->n};
+        BH_CUDA(cudaMemcpyAsync(prm.p, hp, sizeof hp, cudaMemcpyHostToDevice, st));
+        BH_CUDA(cudaMemcpyAsync(dx.p, x, n * sizeof(double), cudaMemcpyHostToDevice, st));
+        if (precision == BH_PREC_FP64) {
+            launch_spmm_shape<double>(op64_of(h), nvec, nvec, prm.p, dx.p, dy.p, st, s);
+        } else {
+            DevBuf<float> fx(n), fy(n);
+            cast_f64_f32(n, dx.p, fx.p, st);
+            launch_spmm_shape<float>(op32_of(h), nvec, nvec, prm.p, fx.p, fy.p, st, s);
+            cast_f32_f64(n, fy.p, dy.p, st);
+        }
+        BH_CUDA(cudaGetLastError());
+        BH_CUDA(cudaMemcpyAsync(y, dy.p, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+        BH_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+int bh_spmm_autotune(const bh_hamiltonian* h, int nvec, int precision, bh_spmm_shape* chosen,
+                     float* ms, float* ms_default) {
+    return guard([&] {
+        BH_REQUIRE(h != nullptr && nvec >= 1, "null argument or nvec < 1");
+        BH_REQUIRE(precision == BH_PREC_FP64 || precision == BH_PREC_MIXED, "unknown precision mode");
+        const int64_t D = h->D, n = D * nvec;
+        Stream st;
+        DevBuf<double> prm(3);
+        const double hp[3] = {1.0, 1.0, 0.0};
+        BH_CUDA(cudaMemcpyAsync(prm.p, hp, sizeof hp, cudaMemcpyHostToDevice, st));
+        TuneEntry e;
+        if (precision == BH_PREC_FP64) {
+            DevBuf<double> X(n), Y(n);
+            BH_CUDA(cudaMemsetAsync(X.p, 0, n * sizeof(double), st));
+            tune_spmm<double>(op64_of(h), nvec, nvec, prm.p, X.p, Y.p, st, false, true, &e);
+            BH_CUDA(cudaStreamSynchronize(st));
+        } else {
+            DevBuf<float> X(n), Y(n);
+            BH_CUDA(cudaMemsetAsync(X.p, 0, n * sizeof(float), st));
+            tune_spmm<float>(op32_of(h), nvec, nvec, prm.p, X.p, Y.p, st, false, true, &e);
+            BH_CUDA(cudaStreamSynchronize(st));
+        }
+        if (chosen) *chosen = shape_out(e.shape);
+        if (ms) *ms = e.ms;
+        if (ms_default) *ms_default = e.ms_default;
+    });
+}
+
+int bh_spmm_tuning_count(int* n) {
+    return guard([&] {
+        BH_REQUIRE(n != nullptr, "null argument");
+        *n = (int)tune_table().size();
+    });
+}
+
+int bh_spmm_tuning_get(int i, bh_spmm_tuning* out) {
+    return guard([&] {
+        BH_REQUIRE(out != nullptr, "null argument");
+        const auto t = tune_table();
+        BH_REQUIRE(i >= 0 && i < (int)t.size(), "tuning entry index out of range");
+        const TuneKey& k = t[(size_t)i].first;
+        const TuneEntry& e = t[(size_t)i].second;
+        out->matrix_free = k.mf;
+        out->elem_bytes = k.elem;
+        out->dim = k.D;
+        out->nnz = k.nnz;
+        out->ncols = e.ncols;
+        out->shape = shape_out(e.shape);
+        out->ms = e.ms;
+        out->ms_default = e.ms_default;
+        out->candidates = e.candidates;
+    });
+}
+
+int bh_spmm_tuning_reset(void) {
+    return guard([&] { tune_reset(); });
+}
+
 }  // extern "C"
+
 
 // ---- mean field ----
 int bh_scmf(int npts, const double* mu, const double* J, int q, const double* psi0, int precision,

@@ -1234,6 +1234,10 @@ struct Launcher {
 
     void spmm(int ncols, int group, const double* prm, const T* X, T* Y, double* dpart = nullptr,
               int* dparts = nullptr) const {
+        // launch shape of this operator and width class, timed at first use
+        // (nothing happens when the table has it, the product fuses, or the
+        // stream is being captured)
+        *launches += tune_spmm<T>(op, ncols, group, prm, X, Y, st, dpart != nullptr);
         profile_begin(st);
         const double bytes = launch_spmm<T>(op, ncols, group, prm, X, Y, st, dpart, dparts);
         done(op.occ ? "k_spmm_mf" : "k_spmm", bytes);
@@ -1665,6 +1669,11 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
                 BH_CUDA(cudaGraphExecDestroy(cg.exec));
                 cg.exec = nullptr;
             }
+            // the products of the captured steps take the tuned shape of this
+            // width: time it now if the table lacks it (W is overwritten by
+            // the cycle's first product before anything reads it)
+            res.launches += tune_spmm<T>(op, ncols, p, d_prm.p, Va.p + (int64_t)jstart * bstride, W.p, st,
+                                         !separate_local_dot());
             const int64_t l0 = res.launches, m0 = res.matvecs;
             cudaGraph_t graph = nullptr;
             BH_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -1927,7 +1936,7 @@ void apply_operator(const OpView<double>& op, int ncols, int group, const double
 // Same product, launched with no profiling events and no host allocation.
 void apply_operator_raw(const OpView<double>& op, int ncols, int group, const double* d_prm,
                         const double* d_X, double* d_Y, cudaStream_t st) {
-    (void)launch_spmm<double>(op, ncols, group, d_prm, d_X, d_Y, st);
+    (void)launch_spmm<double>(op, ncols, group, d_prm, d_X, d_Y, st, nullptr, nullptr, false);
     BH_CUDA(cudaGetLastError());
 }
 

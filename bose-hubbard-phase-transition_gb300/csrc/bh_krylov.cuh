@@ -1,6 +1,8 @@
 // bh_krylov.cuh -- block thick-restart Lanczos on the device (declarations).
 #pragma once
 
+#include <utility>
+
 #include "bh_internal.h"
 
 namespace bh {
@@ -104,6 +106,79 @@ struct SolveResult {
     bool breakdown = false;
 };
 
+// ---------------------------------------------------------------------------
+// Launch shape of the sparse product and its autotuner (bh_spmm_tune.cu).
+//
+// The product runs L lanes per row over the columns (L a power of two <= 32
+// dividing ncols: the row tile is 256 / L rows per CTA), CW columns per lane
+// per pass (the vector block: 1 or 4, also 2 when L = 32; further passes
+// cover the rest of the row's columns), on `grid` CTAs of 256 threads that
+// stride over the rows (0: min(rows / (256 / L), 16 per SM); -1: one
+// resident wave; > 0: that many).  Every shape gives the same Y bit for bit:
+// each column's sum runs over the row's entries (or bonds) in storage order
+// with the same operations, only the thread that computes it changes.  The
+// one exception is the fused CSR product that also yields the partials of
+// V_j^T H V_j, whose CTA partial sums depend on the grid: it keeps its one
+// shape and is never tuned.
+// ---------------------------------------------------------------------------
+struct SpmmShape {
+    int L = 0, CW = 0;
+    int64_t grid = 0;
+};
+
+// A shape relative to the column count, kept by the tuner for a class of
+// widths: L = lmax(ncols) >> dl, CW = 1 if narrow (else the widest that
+// covers the lane's columns in few passes), grid default or one wave.
+struct SpmmChoice {
+    int dl = 0, narrow = 0, wave = 0;
+};
+
+// Largest power of two <= 32 dividing ncols (the default lanes per row).
+int spmm_lmax(int ncols);
+// Concrete shape of a relative choice at ncols ({0, 0, 0} is the default).
+SpmmShape spmm_resolve(const SpmmChoice& c, int ncols);
+// Shapes the tuner times at ncols, the default first, without duplicates.
+std::vector<SpmmChoice> spmm_candidates(int ncols);
+// Whether shape s can run a product of ncols columns.
+bool spmm_shape_valid(const SpmmShape& s, int ncols);
+// Whether the default product fuses the local coefficient (CSR with dpart,
+// block 2 or 4, one pass over the row's columns).
+bool spmm_fuses(bool matrix_free, bool has_dpart, int ncols, int group);
+// Automatic tuning at first use (off with BH_AUTOTUNE=0).
+bool autotune_on();
+
+// One entry of the tuning table: an operator (kind, element size, D, entries)
+// and a class of widths (lmax, passes), the choice and its timings.
+struct TuneKey {
+    int mf = 0, elem = 0, lmax = 0, cls = 0, aux = 0;
+    int64_t D = 0, nnz = 0;
+    bool operator<(const TuneKey& o) const;
+};
+struct TuneEntry {
+    SpmmChoice choice;
+    int ncols = 0;         // width it was timed at
+    SpmmShape shape;       // the choice resolved at that width
+    float ms = 0.f, ms_default = 0.f;
+    int candidates = 0;    // shapes timed
+};
+template <class T>
+TuneKey tune_key(const OpView<T>& op, int ncols) {
+    TuneKey k;
+    k.mf = op.occ ? 1 : 0;
+    k.elem = (int)sizeof(T);
+    k.lmax = spmm_lmax(ncols);
+    const int cpl = ncols / k.lmax;
+    k.cls = cpl <= 1 ? 0 : cpl == 2 ? 1 : cpl <= 4 ? 2 : cpl <= 8 ? 3 : cpl <= 16 ? 4 : 5;
+    k.aux = op.occ ? op.nbonds * 64 + op.m : 0;
+    k.D = op.D;
+    k.nnz = op.rp_nnz;
+    return k;
+}
+bool tune_lookup(const TuneKey& k, SpmmChoice* c);
+void tune_store(const TuneKey& k, const TuneEntry& e);
+std::vector<std::pair<TuneKey, TuneEntry>> tune_table();
+void tune_reset();
+
 // Y = H X for ncols columns of T (CSR operator: MF = false; matrix-free:
 // MF = true), solve of column t = t / group, prm[3 s..] = (J, U, shift);
 // returns the algorithmic bytes.  Instantiated for float and double in
@@ -111,17 +186,53 @@ struct SolveResult {
 // With dpart (CSR operators, block size group = 2 or 4, at most one pass over
 // the row's columns) the product also writes the partial sums of X_s^T Y_s,
 // dpart[(chunk group + q) ncols + t] for chunk < *dparts; *dparts = 0 when
-// the product could not fuse them.
+// the product could not fuse them.  A product that does not fuse takes the
+// tuning table's shape for its operator and width class when `tuned` and
+// the table has one, else the default shape.
 template <class T, bool MF>
 double launch_spmm_kind(const OpView<T>& op, int ncols, int group, const double* prm, const T* X,
-                        T* Y, cudaStream_t st, double* dpart, int* dparts);
+                        T* Y, cudaStream_t st, double* dpart, int* dparts, bool tuned);
+
+// The product (never fused) with a given shape; BH_ERR_ARG if it cannot run.
+template <class T, bool MF>
+double launch_spmm_shape_kind(const OpView<T>& op, int ncols, int group, const double* prm,
+                              const T* X, T* Y, cudaStream_t st, const SpmmShape& s);
+
+// Times the candidate shapes of this operator's width class on the caller's
+// stream and records the fastest, unless the table has the class already
+// (force: time again), the default product fuses (has_dpart), tuning is off
+// (force overrides), or the stream is capturing.  Y is overwritten with H X
+// (the same values as the product itself); X and Y must not overlap.
+// Returns the kernels launched; *out (if given) receives the entry.
+template <class T, bool MF>
+int tune_spmm_kind(const OpView<T>& op, int ncols, int group, const double* prm, const T* X, T* Y,
+                   cudaStream_t st, bool has_dpart, bool force, TuneEntry* out);
 
 template <class T>
 inline double launch_spmm(const OpView<T>& op, int ncols, int group, const double* prm, const T* X,
-                          T* Y, cudaStream_t st, double* dpart = nullptr, int* dparts = nullptr) {
-    return op.occ ? launch_spmm_kind<T, true>(op, ncols, group, prm, X, Y, st, dpart, dparts)
-                  : launch_spmm_kind<T, false>(op, ncols, group, prm, X, Y, st, dpart, dparts);
+                          T* Y, cudaStream_t st, double* dpart = nullptr, int* dparts = nullptr,
+                          bool tuned = true) {
+    return op.occ ? launch_spmm_kind<T, true>(op, ncols, group, prm, X, Y, st, dpart, dparts, tuned)
+                  : launch_spmm_kind<T, false>(op, ncols, group, prm, X, Y, st, dpart, dparts, tuned);
 }
+
+template <class T>
+inline int tune_spmm(const OpView<T>& op, int ncols, int group, const double* prm, const T* X, T* Y,
+                     cudaStream_t st, bool has_dpart, bool force = false, TuneEntry* out = nullptr) {
+    return op.occ ? tune_spmm_kind<T, true>(op, ncols, group, prm, X, Y, st, has_dpart, force, out)
+                  : tune_spmm_kind<T, false>(op, ncols, group, prm, X, Y, st, has_dpart, force, out);
+}
+
+template <class T>
+inline double launch_spmm_shape(const OpView<T>& op, int ncols, int group, const double* prm,
+                                const T* X, T* Y, cudaStream_t st, const SpmmShape& s) {
+    return op.occ ? launch_spmm_shape_kind<T, true>(op, ncols, group, prm, X, Y, st, s)
+                  : launch_spmm_shape_kind<T, false>(op, ncols, group, prm, X, Y, st, s);
+}
+
+// out[i] = in[i] converted, i < n (FP64 <-> FP32 vectors of the shape-forced product).
+void cast_f64_f32(int64_t n, const double* in, float* out, cudaStream_t st);
+void cast_f32_f64(int64_t n, const float* in, double* out, cudaStream_t st);
 
 // Y = H X (FP64) for ncols columns, solve of column t = t / group, prm[3 s..] = (J, U, shift).
 void apply_operator(const OpView<double>& op, int ncols, int group, const double* d_prm,

@@ -293,46 +293,102 @@ int spmm_fused_per_sm() {
     return n;
 }
 
-// Launch of Y = H X on a CSR (MF = false) or matrix-free (MF = true)
-// operator: L lanes per row over the columns (the largest power of two <= 32
-// dividing ncols), CW columns per lane per pass (1 or 2 when that covers the
-// row's share, else 4 with further passes).  For L < 32 the share ncols / L
-// is odd, so only CW in {1, 4} occurs there.  Returns the algorithmic bytes.
+// Dynamic shared memory of the matrix-free product at L lanes per row: the
+// -sqrt table, the rank table and the bonds, plus (L >= 4) the hop lists of
+// the CTA's rows ((256 / L) rows x nbonds x (int32 + T), 16-byte aligned parts).
+template <class T>
+size_t spmm_mf_smem(const OpView<T>& op, int L) {
+    const int nsq = op.n * (op.n + 1) + 1;
+    size_t smem = (((size_t)nsq * sizeof(T) + 15) & ~(size_t)15) +
+                  (size_t)(op.m - 1) * (op.n + 1) * sizeof(uint32_t) + 2 * (size_t)op.nbonds;
+    if (L >= 4) {
+        const size_t nh = (size_t)(256 / L) * op.nbonds;
+        smem = ((smem + 15) & ~(size_t)15) + (nh + (nh & 1)) * 4 + nh * sizeof(T);
+    }
+    return smem;
+}
+
+// Algorithmic bytes of one product: the operator's stream (CSR pattern,
+// values and diagonal, or the packed occupations) plus X read and Y written once.
 template <class T, bool MF>
-double launch_spmm_kind(const OpView<T>& op, int ncols, int group, const double* prm, const T* X,
-                        T* Y, cudaStream_t st, double* dpart, int* dparts) {
-    const int64_t D = op.D;
-    int L = 1;
-    while (L < 32 && L * 2 <= ncols && ncols % (L * 2) == 0) L *= 2;
-    const int cpl = ncols / L;
-    int CW = cpl > 2 ? 4 : cpl;
-    if (L < 32 && CW == 2) CW = 4;
-    const int rpb = 256 / L;
-    int64_t g = (D + rpb - 1) / rpb;
-    g = std::max<int64_t>(1, std::min<int64_t>(g, (int64_t)sm_count() * 16));
-    // fused X^T Y partials: CSR, one pass over the columns, block size 2 or 4
-    const bool fuse = !MF && dpart && (group == 2 || group == 4) && cpl <= CW && L >= group;
-    if (dparts) *dparts = 0;
+double spmm_bytes(const OpView<T>& op, int ncols) {
+    const double D = (double)op.D;
+    if (MF) return D * 8.0 + 2.0 * D * ncols * sizeof(T);
+    const double nnz = (double)op.rp_nnz;
+    return nnz * (4.0 + sizeof(T)) + (D + 1.0) * 8.0 + (op.vd ? D * sizeof(T) : 0.0) +
+           2.0 * D * ncols * sizeof(T);
+}
+
+// Calls f(L, CW) as compile-time constants for the instantiated shapes:
+// CW in {1, 4} for L < 32 (1 when cw == 1, else 4), {1, 2, 4} for L = 32.
+template <class F>
+void by_shape(int L, int cw, F&& f) {
+    auto narrow_or_wide = [&](auto lc) {
+        if (cw == 1) f(lc, std::integral_constant<int, 1>());
+        else f(lc, std::integral_constant<int, 4>());
+    };
+    switch (L) {
+        case 1: narrow_or_wide(std::integral_constant<int, 1>()); break;
+        case 2: narrow_or_wide(std::integral_constant<int, 2>()); break;
+        case 4: narrow_or_wide(std::integral_constant<int, 4>()); break;
+        case 8: narrow_or_wide(std::integral_constant<int, 8>()); break;
+        case 16: narrow_or_wide(std::integral_constant<int, 16>()); break;
+        default:
+            if (cw == 1) f(std::integral_constant<int, 32>(), std::integral_constant<int, 1>());
+            else if (cw == 2) f(std::integral_constant<int, 32>(), std::integral_constant<int, 2>());
+            else f(std::integral_constant<int, 32>(), std::integral_constant<int, 4>());
+            break;
+    }
+}
+
+// The product without the fused partials, with shape s (L, CW from the
+// instantiated set: CW in {1, 4} for L < 32, {1, 2, 4} for L = 32).
+template <class T, bool MF>
+void spmm_launch_plain(const OpView<T>& op, int ncols, int group, const double* prm, const T* X, T* Y,
+                       cudaStream_t st, const SpmmShape& s) {
+    const int64_t rows = (op.D + (256 / s.L) - 1) / (256 / s.L);
     size_t smem = 0;
     if (MF) {
         BH_REQUIRE(op.nbonds <= 128, "matrix-free product: at most 128 directed bonds");
-        const int nsq = op.n * (op.n + 1) + 1;
-        smem = (((size_t)nsq * sizeof(T) + 15) & ~(size_t)15) +
-               (size_t)(op.m - 1) * (op.n + 1) * sizeof(uint32_t) + 2 * (size_t)op.nbonds;
-        if (L >= 4) {  // hop lists: (256 / L) rows x nbonds x (int32 + T), 16-byte aligned parts
-            const size_t nh = (size_t)(256 / L) * op.nbonds;
-            smem = ((smem + 15) & ~(size_t)15) + (nh + (nh & 1)) * 4 + nh * sizeof(T);
-        }
+        smem = spmm_mf_smem(op, s.L);
     }
     auto go = [&](auto lc, auto cwc) {
         constexpr int LL = decltype(lc)::value, CC = decltype(cwc)::value;
-        if constexpr (MF) {
-            auto kern = k_spmm_mf<T, LL, CC>;
+        auto launch = [&](auto kern) {
             allow_large_smem(kern, smem);
-            kern<<<(unsigned)g, 256, smem, st>>>(op, ncols, group, prm, X, Y);
-        }
-        else if (fuse) {
-            // one resident wave (fewer partial rows to reduce, no tail wave)
+            int64_t g = s.grid;
+            if (g == 0) g = std::min<int64_t>(rows, (int64_t)sm_count() * 16);
+            else if (g < 0) g = std::min<int64_t>(rows, (int64_t)sm_count() * std::max(1, resident_ctas(kern, 256, smem)));
+            g = std::max<int64_t>(1, std::min<int64_t>(g, 0x7fffffff));
+            if constexpr (MF) kern<<<(unsigned)g, 256, smem, st>>>(op, ncols, group, prm, X, Y);
+            else kern<<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y, nullptr);
+        };
+        if constexpr (MF) launch(k_spmm_mf<T, LL, CC>);
+        else launch(k_spmm<T, LL, CC, 0>);
+    };
+    by_shape(s.L, s.CW, go);
+}
+
+// Launch of Y = H X on a CSR (MF = false) or matrix-free (MF = true)
+// operator.  Default shape: L lanes per row over the columns (the largest
+// power of two <= 32 dividing ncols), CW columns per lane per pass (1 or 2
+// when that covers the row's share, else 4 with further passes); a product
+// that does not fuse the local coefficient takes the tuning table's shape
+// instead when `tuned` and the table has one.  Returns the algorithmic bytes.
+template <class T, bool MF>
+double launch_spmm_kind(const OpView<T>& op, int ncols, int group, const double* prm, const T* X,
+                        T* Y, cudaStream_t st, double* dpart, int* dparts, bool tuned) {
+    const int64_t D = op.D;
+    const SpmmShape def = spmm_resolve(SpmmChoice{}, ncols);
+    const int L = def.L, CW = def.CW;
+    if (dparts) *dparts = 0;
+    if (spmm_fuses(MF, dpart != nullptr, ncols, group)) {
+        // fused X^T Y partials (CSR, one pass over the columns, block size 2
+        // or 4) on one resident wave (fewer partial rows to reduce, no tail wave)
+        const int rpb = 256 / L;
+        const int64_t g = std::max<int64_t>(1, std::min<int64_t>((D + rpb - 1) / rpb, (int64_t)sm_count() * 16));
+        auto go = [&](auto lc, auto cwc) {
+            constexpr int LL = decltype(lc)::value, CC = decltype(cwc)::value;
             auto fused = [&](auto dpc) {
                 constexpr int DPP = decltype(dpc)::value;
                 const int per_sm = std::min(4, spmm_fused_per_sm<T, LL, CC, DPP>());
@@ -343,30 +399,109 @@ double launch_spmm_kind(const OpView<T>& op, int ncols, int group, const double*
             };
             if (group == 2) fused(std::integral_constant<int, 2>());
             else fused(std::integral_constant<int, 4>());
-        } else {
-            k_spmm<T, LL, CC, 0><<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y, nullptr);
-        }
-    };
-    auto odd_share = [&](auto lc) {
-        if (CW == 1) go(lc, std::integral_constant<int, 1>());
-        else go(lc, std::integral_constant<int, 4>());
-    };
-    switch (L) {
-        case 1: odd_share(std::integral_constant<int, 1>()); break;
-        case 2: odd_share(std::integral_constant<int, 2>()); break;
-        case 4: odd_share(std::integral_constant<int, 4>()); break;
-        case 8: odd_share(std::integral_constant<int, 8>()); break;
-        case 16: odd_share(std::integral_constant<int, 16>()); break;
-        default:
-            if (CW == 1) go(std::integral_constant<int, 32>(), std::integral_constant<int, 1>());
-            else if (CW == 2) go(std::integral_constant<int, 32>(), std::integral_constant<int, 2>());
-            else go(std::integral_constant<int, 32>(), std::integral_constant<int, 4>());
-            break;
+        };
+        if constexpr (!MF) by_shape(L, CW, go);
+        return spmm_bytes<T, MF>(op, ncols);
     }
-    if (MF) return (double)D * 8.0 + 2.0 * (double)D * ncols * sizeof(T);
-    const double nnz = (double)op.rp_nnz;
-    return nnz * (4.0 + sizeof(T)) + (double)(D + 1) * 8.0 + (op.vd ? (double)D * sizeof(T) : 0.0) +
-           2.0 * (double)D * ncols * sizeof(T);
+    SpmmShape s = def;
+    SpmmChoice c;
+    if (tuned && tune_lookup(tune_key(op, ncols), &c)) s = spmm_resolve(c, ncols);
+    spmm_launch_plain<T, MF>(op, ncols, group, prm, X, Y, st, s);
+    return spmm_bytes<T, MF>(op, ncols);
+}
+
+template <class T, bool MF>
+double launch_spmm_shape_kind(const OpView<T>& op, int ncols, int group, const double* prm,
+                              const T* X, T* Y, cudaStream_t st, const SpmmShape& s) {
+    BH_REQUIRE(spmm_shape_valid(s, ncols),
+               "launch shape: lanes must be a power of two <= 32 dividing the column count, "
+               "columns per lane 1 or 4 (or 2 with 32 lanes), grid >= -1");
+    spmm_launch_plain<T, MF>(op, ncols, group, prm, X, Y, st, s);
+    return spmm_bytes<T, MF>(op, ncols);
+}
+
+// Event pair that is destroyed with its scope.
+struct TimerPair {
+    cudaEvent_t a = nullptr, b = nullptr;
+    TimerPair() {
+        BH_CUDA(cudaEventCreate(&a));
+        BH_CUDA(cudaEventCreate(&b));
+    }
+    ~TimerPair() {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+};
+
+template <class T, bool MF>
+int tune_spmm_kind(const OpView<T>& op, int ncols, int group, const double* prm, const T* X, T* Y,
+                   cudaStream_t st, bool has_dpart, bool force, TuneEntry* out) {
+    if (!force && !autotune_on()) return 0;
+    if (op.D < 1 || spmm_fuses(MF, has_dpart, ncols, group)) return 0;
+    const TuneKey key = tune_key(op, ncols);
+    if (!force && tune_lookup(key, nullptr)) return 0;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    BH_CUDA(cudaStreamIsCapturing(st, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return 0;
+
+    const std::vector<SpmmChoice> cands = spmm_candidates(ncols);
+    int launches = 0;
+    // each candidate's kernel once on the first rows only (module loading and
+    // first-launch costs stay out of the timings); rows below 256 of Y get
+    // the values of the full product
+    OpView<T> head = op;
+    head.D = std::min<int64_t>(op.D, 256);
+    for (const SpmmChoice& c : cands) {
+        spmm_launch_plain<T, MF>(head, ncols, group, prm, X, Y, st, spmm_resolve(c, ncols));
+        ++launches;
+    }
+    BH_CUDA(cudaGetLastError());
+    TimerPair ev;
+    auto time_ms = [&](const SpmmShape& s, int reps) {
+        BH_CUDA(cudaEventRecord(ev.a, st));
+        for (int i = 0; i < reps; ++i) spmm_launch_plain<T, MF>(op, ncols, group, prm, X, Y, st, s);
+        BH_CUDA(cudaEventRecord(ev.b, st));
+        BH_CUDA(cudaGetLastError());
+        BH_CUDA(cudaEventSynchronize(ev.b));
+        launches += reps;
+        float ms = 0.f;
+        BH_CUDA(cudaEventElapsedTime(&ms, ev.a, ev.b));
+        return ms / (float)reps;
+    };
+    // the default first; products above 0.25 ms are timed once per shape,
+    // and above 2 ms only the default, one step fewer lanes and one wave run
+    float t_def = time_ms(spmm_resolve(cands[0], ncols), 1);
+    const int reps = t_def < 0.25f ? 3 : 1;
+    if (reps > 1) t_def = std::min(t_def, time_ms(spmm_resolve(cands[0], ncols), reps));
+    const bool expensive = t_def > 2.0f;
+    size_t best = 0;
+    float t_best = t_def;
+    int timed = 1;
+    for (size_t i = 1; i < cands.size(); ++i) {
+        const SpmmChoice& c = cands[i];
+        if (expensive && (c.narrow || c.dl > 1 || (c.dl == 1 && c.wave))) continue;
+        const float t = time_ms(spmm_resolve(c, ncols), reps);
+        ++timed;
+        if (t < t_best) {
+            t_best = t;
+            best = i;
+        }
+    }
+    // keep the default unless another shape is clearly faster (3%)
+    if (best != 0 && t_best > 0.97f * t_def) {
+        best = 0;
+        t_best = t_def;
+    }
+    TuneEntry e;
+    e.choice = cands[best];
+    e.ncols = ncols;
+    e.shape = spmm_resolve(cands[best], ncols);
+    e.ms = t_best;
+    e.ms_default = t_def;
+    e.candidates = timed;
+    tune_store(key, e);
+    if (out) *out = e;
+    return launches;
 }
 
 }  // namespace bh

@@ -4,5 +4,9 @@
 
 namespace bh {
 template double launch_spmm_kind<float, false>(const OpView<float>&, int, int, const double*, const float*,
-                                          float*, cudaStream_t, double*, int*);
+                                          float*, cudaStream_t, double*, int*, bool);
+template double launch_spmm_shape_kind<float, false>(const OpView<float>&, int, int, const double*,
+                                                const float*, float*, cudaStream_t, const SpmmShape&);
+template int tune_spmm_kind<float, false>(const OpView<float>&, int, int, const double*, const float*, float*,
+                                     cudaStream_t, bool, bool, TuneEntry*);
 }  // namespace bh

@@ -4,5 +4,9 @@
 
 namespace bh {
 template double launch_spmm_kind<double, false>(const OpView<double>&, int, int, const double*, const double*,
-                                          double*, cudaStream_t, double*, int*);
+                                          double*, cudaStream_t, double*, int*, bool);
+template double launch_spmm_shape_kind<double, false>(const OpView<double>&, int, int, const double*,
+                                                const double*, double*, cudaStream_t, const SpmmShape&);
+template int tune_spmm_kind<double, false>(const OpView<double>&, int, int, const double*, const double*, double*,
+                                     cudaStream_t, bool, bool, TuneEntry*);
 }  // namespace bh

@@ -280,6 +280,63 @@ int bh_profile_count(int* n);
  * bytes (every operand read once and every result written once). */
 int bh_profile_get(int i, char* name, int name_cap, int64_t* launches, double* ms, double* bytes);
 
+/* ---------------------------------------------------------------------- */
+/* Launch shapes of the sparse product and their autotuner (no counterpart */
+/* in the reference, whose product is Eigen's serial SparseMatrix * vector */
+/* in Spectra's SparseGenMatProd::perform_op, SparseGenMatProd.h:81-86).   */
+/*                                                                         */
+/* The product Y = H X over nvec columns runs `lanes` threads per row      */
+/* (a power of two <= 32 dividing nvec; 256 / lanes rows per CTA),         */
+/* `cols_per_lane` columns per thread per pass (1 or 4, also 2 with 32     */
+/* lanes) on `grid` CTAs of 256 threads striding over the rows (0: the     */
+/* default min(rows / (256 / lanes), 16 per SM); -1: one resident wave).   */
+/* Every shape gives the same y bit for bit.  The solvers time the         */
+/* candidate shapes the first time a width class of an operator is seen    */
+/* (outside any stream capture) and use the fastest from then on; the      */
+/* environment variable BH_AUTOTUNE=0 turns that off.                      */
+/* ---------------------------------------------------------------------- */
+
+typedef struct bh_spmm_shape {
+    int lanes;
+    int cols_per_lane;
+    int64_t grid;
+} bh_spmm_shape;
+
+typedef struct bh_spmm_tuning {
+    int matrix_free;       /* operator kind                                  */
+    int elem_bytes;        /* 4: FP32 vectors (mixed), 8: FP64               */
+    int64_t dim;           /* D                                              */
+    int64_t nnz;           /* off-diagonal entries of T                      */
+    int ncols;             /* width the class was timed at                   */
+    bh_spmm_shape shape;   /* chosen shape at that width                     */
+    float ms;              /* its time per product                           */
+    float ms_default;      /* the default shape's                            */
+    int candidates;        /* shapes timed                                   */
+} bh_spmm_tuning;
+
+/* Candidate shapes for nvec columns, the default first: *count of them are
+ * written to out[0..cap). */
+int bh_spmm_candidates(int nvec, bh_spmm_shape* out, int cap, int* count);
+/* y = H x (lexicographic order, host arrays [D][nvec]) with a given shape
+ * (NULL: the default), in FP64 (BH_PREC_FP64) or with FP32 vectors and
+ * values (BH_PREC_MIXED: x rounded to FP32, y widened back). */
+int bh_hamiltonian_apply_shape(const bh_hamiltonian* h, int precision, double J, double U,
+                               double mu, int nvec, const bh_spmm_shape* shape, const double* x,
+                               double* y);
+/* Times the candidate shapes of products of nvec columns (batches of
+ * nvec / block solves) now, on scratch vectors it allocates, and records the
+ * fastest for this operator's width class (replacing an earlier entry); for
+ * callers that capture their own graphs.  A width whose solver product fuses
+ * the block coefficient (CSR, block 2 or 4, one pass per row) has a single
+ * shape there, but is tuned here all the same for bh_hamiltonian_apply. */
+int bh_spmm_autotune(const bh_hamiltonian* h, int nvec, int precision, bh_spmm_shape* chosen,
+                     float* ms, float* ms_default);
+/* Entries of the process-wide tuning table. */
+int bh_spmm_tuning_count(int* n);
+int bh_spmm_tuning_get(int i, bh_spmm_tuning* out);
+/* Forgets every entry (the next products time their shapes again). */
+int bh_spmm_tuning_reset(void);
+
 #ifdef __cplusplus
 }
 #endif

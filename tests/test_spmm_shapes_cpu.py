@@ -1,0 +1,58 @@
+"""CPU: the launch shapes the autotuner of the sparse product chooses from.
+
+Every candidate must be a shape the library has a kernel for (lanes a power of
+two <= 32 dividing the width, 1 or 4 columns per lane, 2 only with 32 lanes),
+the default shape must come first and equal the fixed rule the product used
+before it had a tuner, and no shape may repeat.  No GPU is touched: these are
+host-only entry points."""
+import ctypes as C
+
+import pytest
+
+
+def default_shape(nvec):
+    L = 1
+    while L < 32 and 2 * L <= nvec and nvec % (2 * L) == 0:
+        L *= 2
+    cpl = nvec // L
+    cw = 4 if cpl > 2 else cpl
+    if L < 32 and cw == 2:
+        cw = 4
+    return (L, cw, 0)
+
+
+@pytest.mark.parametrize("nvec", [1, 2, 3, 4, 6, 10, 12, 20, 32, 60, 63, 64, 96, 126, 128, 256, 512])
+def test_candidates_valid_default_first_unique(pkg, nvec):
+    cands = pkg.spmm_candidates(nvec)
+    assert cands[0] == default_shape(nvec)
+    assert len(set(cands)) == len(cands)
+    assert 1 <= len(cands) <= 12
+    for lanes, cw, grid in cands:
+        assert lanes in (1, 2, 4, 8, 16, 32) and nvec % lanes == 0
+        assert cw in (1, 4) or (cw == 2 and lanes == 32)
+        assert grid in (0, -1)
+    # both grid rules for the default lane count
+    assert (cands[0][0], cands[0][1], -1) in cands
+
+
+def test_candidates_cover_fewer_lanes(pkg):
+    cands = pkg.spmm_candidates(128)
+    lanes = {c[0] for c in cands}
+    assert lanes == {32, 16, 8}
+    # odd multiples of two (batches with an odd number of block-2 solves)
+    lanes = {c[0] for c in pkg.spmm_candidates(126)}
+    assert lanes == {2, 1}
+
+
+def test_candidates_argument_errors(pkg):
+    lib = pkg.load()
+    buf = (pkg.bh_spmm_shape * 2)()
+    n = C.c_int()
+    assert lib.bh_spmm_candidates(0, buf, 2, C.byref(n)) == pkg.BH_ERR_ARG
+    assert lib.bh_spmm_candidates(128, buf, 2, C.byref(n)) == pkg.BH_ERR_ARG  # capacity
+    assert b"capacity" in lib.bh_last_error()
+
+
+def test_tuning_table_starts_empty_and_resets(pkg):
+    pkg.spmm_tuning_reset()
+    assert pkg.spmm_tuning_table() == []
