@@ -11,6 +11,16 @@
 
 namespace bh {
 
+// Explicitly rounded products and fused multiply-adds for the products below:
+// the compiler neither contracts nor splits them, so every launch shape (a
+// different instantiation of the same loops) rounds every entry of Y the
+// same way.  Accumulation: acc = fma(v, x, acc) per entry in storage order;
+// epilogue: y = fma(J, acc, fma(U, d, shift) * x).
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+
 // Y = H X for ncols columns; column t belongs to solve t / group with
 // prm[3 s + 0..2] = (J, U, shift).  L lanes per row, lanes over columns.
 // DP > 0 (= group, one pass over the row's columns): the product also yields
@@ -71,7 +81,7 @@ k_spmm(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
                 for (int k = 0; k < 4; ++k)
 #pragma unroll
                     for (int u = 0; u < CW; ++u)
-                        if (u < nc) acc[u] += vv[k] * xv[k][u];
+                        if (u < nc) acc[u] = fma_rn(vv[k], xv[k][u], acc[u]);
             }
             for (; e < e1; ++e) {
                 const int64_t col = A.ci[e];
@@ -79,7 +89,7 @@ k_spmm(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
                 const T* xr = X + col * ncols + gl + c0 * L;
 #pragma unroll
                 for (int u = 0; u < CW; ++u)
-                    if (u < nc) acc[u] += v * xr[u * L];
+                    if (u < nc) acc[u] = fma_rn(v, xr[u * L], acc[u]);
             }
             T xself[CW], yv[CW];
 #pragma unroll
@@ -91,7 +101,7 @@ k_spmm(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
                     const int s = t / group;
                     const T Jc = (T)prm[3 * s], Uc = (T)prm[3 * s + 1], sh = (T)prm[3 * s + 2];
                     xself[u] = X[r * ncols + t];
-                    yv[u] = Jc * acc[u] + (Uc * d + sh) * xself[u];
+                    yv[u] = fma_rn(Jc, acc[u], mul_rn(fma_rn(Uc, d, sh), xself[u]));
                     Y[r * ncols + t] = yv[u];
                 }
             }
@@ -250,7 +260,7 @@ k_spmm_mf(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
                         if (cc[k] < 0) continue;
 #pragma unroll
                         for (int u = 0; u < CW; ++u)
-                            if (u < nc) acc[u] += vv[k] * xv[k][u];
+                            if (u < nc) acc[u] = fma_rn(vv[k], xv[k][u], acc[u]);
                     }
                 }
             } else {
@@ -263,7 +273,7 @@ k_spmm_mf(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
                     const T* xr = X + c * ncols + gl + c0 * L;
 #pragma unroll
                     for (int u = 0; u < CW; ++u)
-                        if (u < nc) acc[u] += v * xr[u * L];
+                        if (u < nc) acc[u] = fma_rn(v, xr[u * L], acc[u]);
                 }
             }
 #pragma unroll
@@ -273,7 +283,7 @@ k_spmm_mf(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
                     const int s = t / group;
                     const T Jc = (T)prm[3 * s], Uc = (T)prm[3 * s + 1], sh = (T)prm[3 * s + 2];
                     const T xv = X[r * ncols + t];
-                    Y[r * ncols + t] = Jc * acc[u] + (Uc * d + sh) * xv;
+                    Y[r * ncols + t] = fma_rn(Jc, acc[u], mul_rn(fma_rn(Uc, d, sh), xv));
                 }
             }
         }
