@@ -353,18 +353,15 @@ def run_ours(args):
                              for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"]) if v["ms"] > 0}
 
         # launch shapes the autotuner chose for the unfused products of the
-        # bench's sectors (timed during the warm-up steps)
+        # bench's sectors (timed during the first warm-up step, while the five
+        # sectors run concurrently)
         dims = {h.D for h in hams}
         tuned = [e for e in pkg.spmm_tuning_table() if e["dim"] in dims and e["elem_bytes"] == 4]
         if tuned:
             out["spmm_tuning"] = {
                 "width_classes": len(tuned),
-                "non_default_shape": int(sum(e["shape"] != pkg.spmm_candidates(e["ncols"])[0]
-                                             for e in tuned)),
-                "product_time_vs_default": round(sum(e["ms"] for e in tuned) /
-                                                 sum(e["ms_default"] for e in tuned), 4),
-                "definition": "sum over the tuned width classes of the chosen shape's time per "
-                              "product / the default shape's, one product each"}
+                "non_default_shape": int(sum(e["shape"] != pkg.spmm_candidates(e["ncols"], e["matrix_free"])[0]
+                                             for e in tuned))}
 
         rate, cores, secs = cpu_sample_rate()
         out["cpu_baseline"] = {"value": round(rate, 4), "unit": "eigensolves/s", "cores": cores,

@@ -131,7 +131,7 @@ def load() -> C.CDLL:
     L.bh_profile_enable.argtypes = [C.c_int]
     L.bh_profile_count.argtypes = [C.POINTER(C.c_int)]
     L.bh_profile_get.argtypes = [C.c_int, C.c_char_p, C.c_int, i64p, f64p, f64p]
-    L.bh_spmm_candidates.argtypes = [C.c_int, C.POINTER(bh_spmm_shape), C.c_int, C.POINTER(C.c_int)]
+    L.bh_spmm_candidates.argtypes = [C.c_int, C.c_int, C.POINTER(bh_spmm_shape), C.c_int, C.POINTER(C.c_int)]
     L.bh_hamiltonian_apply_shape.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
                                              C.POINTER(bh_spmm_shape), vp, vp]
     L.bh_spmm_autotune.argtypes = [vp, C.c_int, C.c_int, C.POINTER(bh_spmm_shape),
@@ -480,12 +480,13 @@ def profile_read() -> dict:
 # ---------------------------------------------------------------------------
 # launch shapes of the sparse product and the autotuner's table
 # ---------------------------------------------------------------------------
-def spmm_candidates(nvec: int) -> list[tuple[int, int, int]]:
-    """(lanes, cols_per_lane, grid) shapes the tuner times for nvec columns,
-    the default first (grid 0: default, -1: one resident wave)."""
+def spmm_candidates(nvec: int, matrix_free: bool = False) -> list[tuple[int, int, int]]:
+    """(lanes, cols_per_lane, grid) shapes the tuner times for nvec columns of
+    a stored-CSR or matrix-free operator, the default first (grid 0: default,
+    -1: one resident wave)."""
     buf = (bh_spmm_shape * 32)()
     n = C.c_int()
-    _check(load().bh_spmm_candidates(nvec, buf, 32, C.byref(n)))
+    _check(load().bh_spmm_candidates(nvec, int(bool(matrix_free)), buf, 32, C.byref(n)))
     return [(buf[i].lanes, buf[i].cols_per_lane, buf[i].grid) for i in range(n.value)]
 
 

@@ -627,12 +627,13 @@ static bh_spmm_shape shape_out(const SpmmShape& s) {
     return o;
 }
 
-int bh_spmm_candidates(int nvec, bh_spmm_shape* out, int cap, int* count) {
+int bh_spmm_candidates(int nvec, int matrix_free, bh_spmm_shape* out, int cap, int* count) {
     return guard([&] {
         BH_REQUIRE(nvec >= 1 && count, "null argument or nvec < 1");
-        const std::vector<SpmmChoice> c = spmm_candidates(nvec);
+        const bool mf = matrix_free != 0;
+        const std::vector<SpmmChoice> c = spmm_candidates(nvec, mf);
         BH_REQUIRE(cap >= (int)c.size() && out, "output capacity too small");
-        for (size_t i = 0; i < c.size(); ++i) out[i] = shape_out(spmm_resolve(c[i], nvec));
+        for (size_t i = 0; i < c.size(); ++i) out[i] = shape_out(spmm_resolve(c[i], nvec, mf));
         *count = (int)c.size();
     });
 }
@@ -643,10 +644,11 @@ int bh_hamiltonian_apply_shape(const bh_hamiltonian* h, int precision, double J,
     return guard([&] {
         BH_REQUIRE(h != nullptr && x && y && nvec >= 1, "null argument");
         BH_REQUIRE(precision == BH_PREC_FP64 || precision == BH_PREC_MIXED, "unknown precision mode");
-        const SpmmShape s = shape ? shape_in(*shape) : spmm_resolve(SpmmChoice{}, nvec);
-        BH_REQUIRE(spmm_shape_valid(s, nvec),
-                   "launch shape: lanes must be a power of two <= 32 dividing nvec, columns per "
-                   "lane 1 or 4 (or 2 with 32 lanes), grid >= -1");
+        const SpmmShape s = shape ? shape_in(*shape) : spmm_resolve(SpmmChoice{}, nvec, h->matrix_free);
+        BH_REQUIRE(spmm_shape_valid(s, nvec, h->matrix_free),
+                   "launch shape: lanes must be a power of two <= 32 dividing nvec (32 at any nvec "
+                   "for a matrix-free operator), columns per lane 1 or 4 (or 2 with 32 lanes), "
+                   "grid >= -1");
         const int64_t D = h->D, n = D * nvec;
         Stream st;
         DevBuf<double> dx(n), dy(n), prm(3);

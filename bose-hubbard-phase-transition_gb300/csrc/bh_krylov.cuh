@@ -126,9 +126,14 @@ struct SpmmShape {
     int64_t grid = 0;
 };
 
+// The matrix-free product also has a warp-per-row kernel (L = 32 at any
+// ncols, columns t = lane + 32 u masked by t < ncols), its default shape.
+//
 // A shape relative to the column count, kept by the tuner for a class of
-// widths: L = lmax(ncols) >> dl, CW = 1 if narrow (else the widest that
-// covers the lane's columns in few passes), grid default or one wave.
+// widths: L = lmax(ncols) >> dl (matrix-free: dl = 0 is the warp kernel,
+// dl >= 1 the per-lane kernels from lmax, or 16 when lmax = 32, down), CW = 1
+// if narrow (else the widest that covers the lane's columns in few passes),
+// grid default or one wave.
 struct SpmmChoice {
     int dl = 0, narrow = 0, wave = 0;
 };
@@ -136,11 +141,11 @@ struct SpmmChoice {
 // Largest power of two <= 32 dividing ncols (the default lanes per row).
 int spmm_lmax(int ncols);
 // Concrete shape of a relative choice at ncols ({0, 0, 0} is the default).
-SpmmShape spmm_resolve(const SpmmChoice& c, int ncols);
+SpmmShape spmm_resolve(const SpmmChoice& c, int ncols, bool matrix_free = false);
 // Shapes the tuner times at ncols, the default first, without duplicates.
-std::vector<SpmmChoice> spmm_candidates(int ncols);
+std::vector<SpmmChoice> spmm_candidates(int ncols, bool matrix_free = false);
 // Whether shape s can run a product of ncols columns.
-bool spmm_shape_valid(const SpmmShape& s, int ncols);
+bool spmm_shape_valid(const SpmmShape& s, int ncols, bool matrix_free = false);
 // Whether the default product fuses the local coefficient (CSR with dpart,
 // block 2 or 4, one pass over the row's columns).
 bool spmm_fuses(bool matrix_free, bool has_dpart, int ncols, int group);
@@ -167,8 +172,8 @@ TuneKey tune_key(const OpView<T>& op, int ncols) {
     k.mf = op.occ ? 1 : 0;
     k.elem = (int)sizeof(T);
     k.lmax = spmm_lmax(ncols);
-    const int cpl = ncols / k.lmax;
-    k.cls = cpl <= 1 ? 0 : cpl == 2 ? 1 : cpl <= 4 ? 2 : cpl <= 8 ? 3 : cpl <= 16 ? 4 : 5;
+    auto bucket = [](int c) { return c <= 1 ? 0 : c == 2 ? 1 : c <= 4 ? 2 : c <= 8 ? 3 : c <= 16 ? 4 : 5; };
+    k.cls = bucket(ncols / k.lmax) + (op.occ ? 8 * bucket((ncols + 31) / 32) : 0);
     k.aux = op.occ ? op.nbonds * 64 + op.m : 0;
     k.D = op.D;
     k.nnz = op.rp_nnz;

@@ -291,6 +291,163 @@ k_spmm_mf(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
     }
 }
 
+// Four consecutive hop values of a row's list (16-byte aligned).
+__device__ __forceinline__ void load4(const float* p, float (&v)[4]) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    v[0] = q.x;
+    v[1] = q.y;
+    v[2] = q.z;
+    v[3] = q.w;
+}
+__device__ __forceinline__ void load4(const double* p, double (&v)[4]) {
+    const double2 a = *reinterpret_cast<const double2*>(p);
+    const double2 b = *reinterpret_cast<const double2*>(p + 2);
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = b.x;
+    v[3] = b.y;
+}
+
+// Matrix-free product with one warp per row (8 rows per CTA), for any ncols:
+// lane l computes columns t = l + 32 u (u < CW per pass, t < ncols).  The
+// row's integer work is spread over the lanes (m <= 32 sites): lane t
+// extracts n_t, the suffix sums s_t = sum_{u > t} n_u and the interaction
+// sum come from warp scans, and the rank of the state after a hop i -> j is
+//   r + (P_a[j] - P_a[i])   (i < j),   r - (P_b[i] - P_b[j])   (i > j),
+// with exclusive prefix sums over sites of the rank increments
+//   a_t = RT[t][s_t + 1] - RT[t][s_t],   b_t = RT[t][s_t] - RT[t][s_t - 1]
+// (one boson crossing the cut after site t raises or lowers s_t by one; sums
+// modulo 2^32, the true difference is below D in magnitude), so a bond costs
+// a few shuffles instead of |i - j| rank-table lookups.  The valid hops
+// (n_i >= 1) are compacted in bond order into the warp's shared-memory list
+// and summed in that order, as the other matrix-free paths do: Y is the same
+// bit for bit.
+template <class T, int CW>
+__global__ void __launch_bounds__(256)
+k_spmm_mf_warp(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
+               const T* __restrict__ X, T* __restrict__ Y) {
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    constexpr unsigned FULL = 0xffffffffu;
+    const int m = A.m, n = A.n, nb = A.nbonds, bits = A.bits;
+    const int nrt = (m - 1) * (n + 1), nsq = n * (n + 1) + 1;
+    const int nbp = (nb + 3) & ~3;
+    T* s_sq = reinterpret_cast<T*>(s_raw);
+    uint32_t* s_rt = reinterpret_cast<uint32_t*>(s_raw + (((size_t)nsq * sizeof(T) + 15) & ~(size_t)15));
+    uint8_t* s_bd = reinterpret_cast<uint8_t*>(s_rt + nrt);
+    const size_t hop_off =
+        ((((size_t)nsq * sizeof(T) + 15) & ~(size_t)15) + (size_t)nrt * 4 + 2 * (size_t)nb + 15) & ~(size_t)15;
+    int32_t* s_hc = reinterpret_cast<int32_t*>(s_raw + hop_off);
+    T* s_hv = reinterpret_cast<T*>(s_raw + hop_off + (size_t)8 * nbp * sizeof(int32_t));
+    for (int i = threadIdx.x; i < nsq; i += blockDim.x) s_sq[i] = A.sq[i];
+    for (int i = threadIdx.x; i < nrt; i += blockDim.x) s_rt[i] = A.rt[i];
+    for (int i = threadIdx.x; i < 2 * nb; i += blockDim.x) s_bd[i] = A.bonds[i];
+    __syncthreads();
+    const uint64_t mask = (1ull << bits) - 1ull;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int32_t* hc = s_hc + warp * nbp;
+    T* hv = s_hv + warp * nbp;
+    const int cpl = (ncols + 31) >> 5;
+    // every lane of a warp walks the same rows: the shuffles below are uniform
+    for (int64_t r = (int64_t)blockIdx.x * 8 + warp; r < A.D; r += (int64_t)gridDim.x * 8) {
+        const uint64_t w = A.occ[r];
+        const int nt = lane < m ? (int)((w >> (bits * lane)) & mask) : 0;
+        int suf = nt;  // inclusive suffix sum over lanes >= this one
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_down_sync(FULL, suf, o);
+            if (lane + o < 32) suf += v;
+        }
+        const int st = suf - nt;
+        int v2 = nt * (nt - 1);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v2 += __shfl_xor_sync(FULL, v2, o);
+        const T d = (T)(0.5 * (double)v2);
+        uint32_t a = 0, b = 0;
+        if (lane < m - 1) {
+            const uint32_t* rt = s_rt + lane * (n + 1);
+            if (st < n) a = rt[st + 1] - rt[st];
+            if (st > 0) b = rt[st] - rt[st - 1];
+        }
+        uint32_t pa = a, pb = b;  // inclusive prefix sums, then exclusive
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t ua = __shfl_up_sync(FULL, pa, o), ub = __shfl_up_sync(FULL, pb, o);
+            if (lane >= o) {
+                pa += ua;
+                pb += ub;
+            }
+        }
+        pa -= a;
+        pb -= b;
+        // hop list of the row: bonds k = k0 + lane, valid ones compacted in order
+        int cnt = 0;
+        for (int k0 = 0; k0 < nb; k0 += 32) {
+            const int k = k0 + lane;
+            int i = 0, j = 0;
+            if (k < nb) {
+                i = s_bd[2 * k];
+                j = s_bd[2 * k + 1];
+            }
+            const int ni = __shfl_sync(FULL, nt, i), nj = __shfl_sync(FULL, nt, j);
+            const uint32_t pai = __shfl_sync(FULL, pa, i), paj = __shfl_sync(FULL, pa, j);
+            const uint32_t pbi = __shfl_sync(FULL, pb, i), pbj = __shfl_sync(FULL, pb, j);
+            const bool ok = k < nb && ni >= 1;
+            const unsigned bal = __ballot_sync(FULL, ok);
+            if (ok) {
+                const int32_t dr = i < j ? (int32_t)(paj - pai) : -(int32_t)(pbi - pbj);
+                const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
+                hc[pos] = (int32_t)r + dr;
+                hv[pos] = s_sq[ni * (nj + 1)];
+            }
+            cnt += __popc(bal);
+        }
+        __syncwarp();
+        for (int c0 = 0; c0 < cpl; c0 += CW) {
+            T acc[CW];
+            bool on[CW];
+#pragma unroll
+            for (int u = 0; u < CW; ++u) {
+                acc[u] = T(0);
+                on[u] = c0 + u < cpl && lane + 32 * (c0 + u) < ncols;
+            }
+            // bonds in order, four per step: the four X rows are requested
+            // before the first product
+            for (int e = 0; e < cnt; e += 4) {
+                const int4 c4 = *reinterpret_cast<const int4*>(hc + e);
+                const int cc[4] = {c4.x, c4.y, c4.z, c4.w};
+                T vv[4], xv[4][CW];
+                load4(hv + e, vv);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    if (e + k >= cnt) continue;
+                    const T* xr = X + (int64_t)cc[k] * ncols + lane + 32 * c0;
+#pragma unroll
+                    for (int u = 0; u < CW; ++u)
+                        if (on[u]) xv[k][u] = xr[32 * u];
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    if (e + k >= cnt) continue;
+#pragma unroll
+                    for (int u = 0; u < CW; ++u)
+                        if (on[u]) acc[u] = fma_rn(vv[k], xv[k][u], acc[u]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < CW; ++u) {
+                if (on[u]) {
+                    const int t = lane + 32 * (c0 + u);
+                    const int s = t / group;
+                    const T Jc = (T)prm[3 * s], Uc = (T)prm[3 * s + 1], sh = (T)prm[3 * s + 2];
+                    const T xv = X[r * ncols + t];
+                    Y[r * ncols + t] = fma_rn(Jc, acc[u], mul_rn(fma_rn(Uc, d, sh), xv));
+                }
+            }
+        }
+        __syncwarp();  // the next row overwrites the hop list
+    }
+}
+
 // Resident CTAs per SM of the fused CSR product (found once per instance).
 template <class T, int L, int CW, int DP>
 int spmm_fused_per_sm() {
@@ -316,6 +473,19 @@ size_t spmm_mf_smem(const OpView<T>& op, int L) {
         smem = ((smem + 15) & ~(size_t)15) + (nh + (nh & 1)) * 4 + nh * sizeof(T);
     }
     return smem;
+}
+
+// Dynamic shared memory of the warp-per-row matrix-free product: the same
+// tables, then the hop lists of its 8 rows, padded to 4 entries (int32 row
+// indices, then the values).
+template <class T>
+size_t spmm_mf_warp_smem(const OpView<T>& op) {
+    const int nsq = op.n * (op.n + 1) + 1;
+    const size_t nbp = ((size_t)op.nbonds + 3) & ~(size_t)3;
+    size_t smem = (((size_t)nsq * sizeof(T) + 15) & ~(size_t)15) +
+                  (size_t)(op.m - 1) * (op.n + 1) * sizeof(uint32_t) + 2 * (size_t)op.nbonds;
+    smem = (smem + 15) & ~(size_t)15;
+    return smem + 8 * nbp * (sizeof(int32_t) + sizeof(T));
 }
 
 // Algorithmic bytes of one product: the operator's stream (CSR pattern,
@@ -360,7 +530,8 @@ void spmm_launch_plain(const OpView<T>& op, int ncols, int group, const double* 
     size_t smem = 0;
     if (MF) {
         BH_REQUIRE(op.nbonds <= 128, "matrix-free product: at most 128 directed bonds");
-        smem = spmm_mf_smem(op, s.L);
+        BH_REQUIRE(op.m <= 32, "matrix-free product: at most 32 sites");
+        smem = s.L == 32 ? spmm_mf_warp_smem(op) : spmm_mf_smem(op, s.L);
     }
     auto go = [&](auto lc, auto cwc) {
         constexpr int LL = decltype(lc)::value, CC = decltype(cwc)::value;
@@ -373,7 +544,8 @@ void spmm_launch_plain(const OpView<T>& op, int ncols, int group, const double* 
             if constexpr (MF) kern<<<(unsigned)g, 256, smem, st>>>(op, ncols, group, prm, X, Y);
             else kern<<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y, nullptr);
         };
-        if constexpr (MF) launch(k_spmm_mf<T, LL, CC>);
+        if constexpr (MF && LL == 32) launch(k_spmm_mf_warp<T, CC>);
+        else if constexpr (MF) launch(k_spmm_mf<T, LL, CC>);
         else launch(k_spmm<T, LL, CC, 0>);
     };
     by_shape(s.L, s.CW, go);
@@ -389,7 +561,7 @@ template <class T, bool MF>
 double launch_spmm_kind(const OpView<T>& op, int ncols, int group, const double* prm, const T* X,
                         T* Y, cudaStream_t st, double* dpart, int* dparts, bool tuned) {
     const int64_t D = op.D;
-    const SpmmShape def = spmm_resolve(SpmmChoice{}, ncols);
+    const SpmmShape def = spmm_resolve(SpmmChoice{}, ncols, MF);
     const int L = def.L, CW = def.CW;
     if (dparts) *dparts = 0;
     if (spmm_fuses(MF, dpart != nullptr, ncols, group)) {
@@ -415,7 +587,7 @@ double launch_spmm_kind(const OpView<T>& op, int ncols, int group, const double*
     }
     SpmmShape s = def;
     SpmmChoice c;
-    if (tuned && tune_lookup(tune_key(op, ncols), &c)) s = spmm_resolve(c, ncols);
+    if (tuned && tune_lookup(tune_key(op, ncols), &c)) s = spmm_resolve(c, ncols, MF);
     spmm_launch_plain<T, MF>(op, ncols, group, prm, X, Y, st, s);
     return spmm_bytes<T, MF>(op, ncols);
 }
@@ -423,9 +595,10 @@ double launch_spmm_kind(const OpView<T>& op, int ncols, int group, const double*
 template <class T, bool MF>
 double launch_spmm_shape_kind(const OpView<T>& op, int ncols, int group, const double* prm,
                               const T* X, T* Y, cudaStream_t st, const SpmmShape& s) {
-    BH_REQUIRE(spmm_shape_valid(s, ncols),
-               "launch shape: lanes must be a power of two <= 32 dividing the column count, "
-               "columns per lane 1 or 4 (or 2 with 32 lanes), grid >= -1");
+    BH_REQUIRE(spmm_shape_valid(s, ncols, MF),
+               "launch shape: lanes must be a power of two <= 32 dividing the column count "
+               "(32 at any count for the matrix-free product), columns per lane 1 or 4 (or 2 "
+               "with 32 lanes), grid >= -1");
     spmm_launch_plain<T, MF>(op, ncols, group, prm, X, Y, st, s);
     return spmm_bytes<T, MF>(op, ncols);
 }
@@ -454,7 +627,7 @@ int tune_spmm_kind(const OpView<T>& op, int ncols, int group, const double* prm,
     BH_CUDA(cudaStreamIsCapturing(st, &cs));
     if (cs != cudaStreamCaptureStatusNone) return 0;
 
-    const std::vector<SpmmChoice> cands = spmm_candidates(ncols);
+    const std::vector<SpmmChoice> cands = spmm_candidates(ncols, MF);
     int launches = 0;
     // each candidate's kernel once on the first rows only (module loading and
     // first-launch costs stay out of the timings); rows below 256 of Y get
@@ -462,27 +635,33 @@ int tune_spmm_kind(const OpView<T>& op, int ncols, int group, const double* prm,
     OpView<T> head = op;
     head.D = std::min<int64_t>(op.D, 256);
     for (const SpmmChoice& c : cands) {
-        spmm_launch_plain<T, MF>(head, ncols, group, prm, X, Y, st, spmm_resolve(c, ncols));
+        spmm_launch_plain<T, MF>(head, ncols, group, prm, X, Y, st, spmm_resolve(c, ncols, MF));
         ++launches;
     }
     BH_CUDA(cudaGetLastError());
     TimerPair ev;
+    // the fastest of `reps` separately timed launches (products of other
+    // streams running at the same time only ever lengthen a launch)
     auto time_ms = [&](const SpmmShape& s, int reps) {
-        BH_CUDA(cudaEventRecord(ev.a, st));
-        for (int i = 0; i < reps; ++i) spmm_launch_plain<T, MF>(op, ncols, group, prm, X, Y, st, s);
-        BH_CUDA(cudaEventRecord(ev.b, st));
-        BH_CUDA(cudaGetLastError());
-        BH_CUDA(cudaEventSynchronize(ev.b));
+        float best = 0.f;
+        for (int i = 0; i < reps; ++i) {
+            BH_CUDA(cudaEventRecord(ev.a, st));
+            spmm_launch_plain<T, MF>(op, ncols, group, prm, X, Y, st, s);
+            BH_CUDA(cudaEventRecord(ev.b, st));
+            BH_CUDA(cudaGetLastError());
+            BH_CUDA(cudaEventSynchronize(ev.b));
+            float ms = 0.f;
+            BH_CUDA(cudaEventElapsedTime(&ms, ev.a, ev.b));
+            best = i == 0 ? ms : std::min(best, ms);
+        }
         launches += reps;
-        float ms = 0.f;
-        BH_CUDA(cudaEventElapsedTime(&ms, ev.a, ev.b));
-        return ms / (float)reps;
+        return best;
     };
     // the default first; products above 0.25 ms are timed once per shape,
     // and above 2 ms only the default, one step fewer lanes and one wave run
-    float t_def = time_ms(spmm_resolve(cands[0], ncols), 1);
+    float t_def = time_ms(spmm_resolve(cands[0], ncols, MF), 1);
     const int reps = t_def < 0.25f ? 3 : 1;
-    if (reps > 1) t_def = std::min(t_def, time_ms(spmm_resolve(cands[0], ncols), reps));
+    if (reps > 1) t_def = std::min(t_def, time_ms(spmm_resolve(cands[0], ncols, MF), reps));
     const bool expensive = t_def > 2.0f;
     size_t best = 0;
     float t_best = t_def;
@@ -490,7 +669,7 @@ int tune_spmm_kind(const OpView<T>& op, int ncols, int group, const double* prm,
     for (size_t i = 1; i < cands.size(); ++i) {
         const SpmmChoice& c = cands[i];
         if (expensive && (c.narrow || c.dl > 1 || (c.dl == 1 && c.wave))) continue;
-        const float t = time_ms(spmm_resolve(c, ncols), reps);
+        const float t = time_ms(spmm_resolve(c, ncols, MF), reps);
         ++timed;
         if (t < t_best) {
             t_best = t;
@@ -505,7 +684,7 @@ int tune_spmm_kind(const OpView<T>& op, int ncols, int group, const double* prm,
     TuneEntry e;
     e.choice = cands[best];
     e.ncols = ncols;
-    e.shape = spmm_resolve(cands[best], ncols);
+    e.shape = spmm_resolve(cands[best], ncols, MF);
     e.ms = t_best;
     e.ms_default = t_def;
     e.candidates = timed;

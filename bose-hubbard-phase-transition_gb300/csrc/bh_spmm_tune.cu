@@ -25,29 +25,44 @@ int spmm_lmax(int ncols) {
     return L;
 }
 
-SpmmShape spmm_resolve(const SpmmChoice& c, int ncols) {
+// Columns per lane of the wide choice for cpl columns per lane in all.
+static int wide_cw(int L, int cpl) {
+    if (cpl <= 1) return 1;
+    if (cpl == 2) return L == 32 ? 2 : 4;
+    return 4;
+}
+
+SpmmShape spmm_resolve(const SpmmChoice& c, int ncols, bool matrix_free) {
     SpmmShape s;
-    int L = spmm_lmax(ncols) >> c.dl;
-    if (L < 1) L = 1;
-    const int cpl = ncols / L;
+    const int lmax = spmm_lmax(ncols);
+    int L, cpl;
+    if (matrix_free && c.dl == 0) {
+        L = 32;  // warp per row, masked columns
+        cpl = (ncols + 31) / 32;
+    } else {
+        const int top = matrix_free ? (lmax == 32 ? 16 : lmax) : lmax;
+        L = top >> (matrix_free ? c.dl - 1 : c.dl);
+        if (L < 1) L = 1;
+        cpl = ncols / L;
+    }
     s.L = L;
-    if (c.narrow || cpl <= 1) s.CW = 1;
-    else if (cpl == 2) s.CW = L == 32 ? 2 : 4;
-    else s.CW = 4;
+    s.CW = c.narrow ? 1 : wide_cw(L, cpl);
     s.grid = c.wave ? -1 : 0;
     return s;
 }
 
-std::vector<SpmmChoice> spmm_candidates(int ncols) {
+std::vector<SpmmChoice> spmm_candidates(int ncols, bool matrix_free) {
     std::vector<SpmmChoice> out;
     std::vector<std::tuple<int, int, int64_t>> seen;
     const int lmax = spmm_lmax(ncols);
+    const int top = matrix_free ? (lmax == 32 ? 16 : lmax) : lmax;
     for (int wave = 0; wave < 2; ++wave)
         for (int dl = 0; dl < 3; ++dl) {
-            if ((lmax >> dl) < 1) continue;
+            const int shift = matrix_free ? dl - 1 : dl;
+            if (shift >= 0 && (top >> shift) < 1) continue;
             for (int narrow = 0; narrow < 2; ++narrow) {
                 const SpmmChoice c{dl, narrow, wave};
-                const SpmmShape s = spmm_resolve(c, ncols);
+                const SpmmShape s = spmm_resolve(c, ncols, matrix_free);
                 const auto t = std::make_tuple(s.L, s.CW, s.grid);
                 if (std::find(seen.begin(), seen.end(), t) != seen.end()) continue;
                 seen.push_back(t);
@@ -57,17 +72,17 @@ std::vector<SpmmChoice> spmm_candidates(int ncols) {
     return out;
 }
 
-bool spmm_shape_valid(const SpmmShape& s, int ncols) {
-    if (ncols < 1) return false;
+bool spmm_shape_valid(const SpmmShape& s, int ncols, bool matrix_free) {
+    if (ncols < 1 || s.grid < -1) return false;
     if (!(s.L == 1 || s.L == 2 || s.L == 4 || s.L == 8 || s.L == 16 || s.L == 32)) return false;
-    if (ncols % s.L != 0) return false;
     if (!(s.CW == 1 || s.CW == 4 || (s.CW == 2 && s.L == 32))) return false;
-    return s.grid >= -1;
+    if (matrix_free && s.L == 32) return true;  // warp per row, masked columns
+    return ncols % s.L == 0;
 }
 
 bool spmm_fuses(bool matrix_free, bool has_dpart, int ncols, int group) {
     if (matrix_free || !has_dpart || !(group == 2 || group == 4) || ncols < 1) return false;
-    const SpmmShape d = spmm_resolve(SpmmChoice{}, ncols);
+    const SpmmShape d = spmm_resolve(SpmmChoice{}, ncols, false);
     return ncols / d.L <= d.CW && d.L >= group;
 }
 

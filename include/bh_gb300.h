@@ -286,7 +286,9 @@ int bh_profile_get(int i, char* name, int name_cap, int64_t* launches, double* m
 /* in Spectra's SparseGenMatProd::perform_op, SparseGenMatProd.h:81-86).   */
 /*                                                                         */
 /* The product Y = H X over nvec columns runs `lanes` threads per row      */
-/* (a power of two <= 32 dividing nvec; 256 / lanes rows per CTA),         */
+/* (a power of two <= 32 dividing nvec; 256 / lanes rows per CTA; the      */
+/* matrix-free product also runs one warp per row, lanes = 32, at any      */
+/* nvec, its default),                                                     */
 /* `cols_per_lane` columns per thread per pass (1 or 4, also 2 with 32     */
 /* lanes) on `grid` CTAs of 256 threads striding over the rows (0: the     */
 /* default min(rows / (256 / lanes), 16 per SM); -1: one resident wave).   */
@@ -314,9 +316,10 @@ typedef struct bh_spmm_tuning {
     int candidates;        /* shapes timed                                   */
 } bh_spmm_tuning;
 
-/* Candidate shapes for nvec columns, the default first: *count of them are
- * written to out[0..cap). */
-int bh_spmm_candidates(int nvec, bh_spmm_shape* out, int cap, int* count);
+/* Candidate shapes for nvec columns of a stored-CSR (matrix_free = 0) or
+ * matrix-free operator, the default first: *count of them are written to
+ * out[0..cap). */
+int bh_spmm_candidates(int nvec, int matrix_free, bh_spmm_shape* out, int cap, int* count);
 /* y = H x (lexicographic order, host arrays [D][nvec]) with a given shape
  * (NULL: the default), in FP64 (BH_PREC_FP64) or with FP32 vectors and
  * values (BH_PREC_MIXED: x rounded to FP32, y widened back). */

@@ -10,7 +10,11 @@ import ctypes as C
 import pytest
 
 
-def default_shape(nvec):
+def default_shape(nvec, matrix_free=False):
+    if matrix_free:
+        # one warp per row, columns masked: 1, 2 or 4 columns per lane per pass
+        cpl = (nvec + 31) // 32
+        return (32, 1 if cpl == 1 else 2 if cpl == 2 else 4, 0)
     L = 1
     while L < 32 and 2 * L <= nvec and nvec % (2 * L) == 0:
         L *= 2
@@ -35,6 +39,19 @@ def test_candidates_valid_default_first_unique(pkg, nvec):
     assert (cands[0][0], cands[0][1], -1) in cands
 
 
+@pytest.mark.parametrize("nvec", [1, 2, 3, 12, 28, 60, 63, 64, 100, 128, 512])
+def test_matrix_free_candidates(pkg, nvec):
+    cands = pkg.spmm_candidates(nvec, True)
+    assert cands[0] == default_shape(nvec, True)
+    assert len(set(cands)) == len(cands) and len(cands) <= 12
+    for lanes, cw, grid in cands:
+        # 32 lanes is the warp-per-row kernel, at any width; fewer lanes must divide it
+        assert lanes == 32 or nvec % lanes == 0
+        assert cw in (1, 4) or (cw == 2 and lanes == 32)
+    # the per-lane kernels stay candidates
+    assert any(c[0] < 32 for c in cands) or nvec == 1
+
+
 def test_candidates_cover_fewer_lanes(pkg):
     cands = pkg.spmm_candidates(128)
     lanes = {c[0] for c in cands}
@@ -48,8 +65,8 @@ def test_candidates_argument_errors(pkg):
     lib = pkg.load()
     buf = (pkg.bh_spmm_shape * 2)()
     n = C.c_int()
-    assert lib.bh_spmm_candidates(0, buf, 2, C.byref(n)) == pkg.BH_ERR_ARG
-    assert lib.bh_spmm_candidates(128, buf, 2, C.byref(n)) == pkg.BH_ERR_ARG  # capacity
+    assert lib.bh_spmm_candidates(0, 0, buf, 2, C.byref(n)) == pkg.BH_ERR_ARG
+    assert lib.bh_spmm_candidates(128, 0, buf, 2, C.byref(n)) == pkg.BH_ERR_ARG  # capacity
     assert b"capacity" in lib.bh_last_error()
 
 

@@ -22,7 +22,7 @@ from conftest import ROOT, chain_lists
 
 pytestmark = pytest.mark.gpu
 
-WIDTHS = [1, 2, 6, 12, 64, 128]
+WIDTHS = [1, 2, 6, 12, 28, 60, 64, 128]
 
 
 def square_lists(pkg, m):
@@ -48,9 +48,12 @@ def test_every_shape_gives_the_default_product_bit_for_bit(pkg, prec):
                 # the allocating lexicographic apply (default or tuned shape)
                 ya = h.apply(x, 0.11, 1.0, 0.3, order=pkg.ORDER_LEX)
                 assert np.array_equal(ya, y0), (name, nvec)
-            shapes = pkg.spmm_candidates(nvec)
+            shapes = pkg.spmm_candidates(nvec, h.matrix_free)
             L0, c0, _ = shapes[0]
             shapes += [(L0, c0, 1), (L0, c0, 7), (1, 1, 3)]
+            if h.matrix_free:
+                # the warp-per-row kernel at every column width, one and several passes
+                shapes += [(32, 1, 0), (32, 2, 5), (32, 4, -1)]
             for s in shapes:
                 y = h.apply_shape(x, 0.11, 1.0, 0.3, s, precision=p)
                 assert np.array_equal(y, y0), (name, nvec, s)
@@ -71,12 +74,12 @@ def test_explicit_autotune_records_an_entry(pkg):
     y0 = h.apply_shape(x, 0.2, 1.0, 0.1, None)
     for prec in (pkg.PREC_MIXED, pkg.PREC_FP64):
         r = h.autotune(46, precision=prec)
-        assert r["shape"] in pkg.spmm_candidates(46)
+        assert r["shape"] in pkg.spmm_candidates(46, False)
         assert 0.0 < r["ms"] <= r["ms_default"]
     tab = pkg.spmm_tuning_table()
     assert {e["elem_bytes"] for e in tab if e["dim"] == h.D} == {4, 8}
     for e in tab:
-        assert e["candidates"] >= 1 and e["shape"] in pkg.spmm_candidates(e["ncols"])
+        assert e["candidates"] >= 1 and e["shape"] in pkg.spmm_candidates(e["ncols"], e["matrix_free"])
     # the FP64 apply now takes the tuned shape: same values
     assert np.array_equal(h.apply(x, 0.2, 1.0, 0.1, order=pkg.ORDER_LEX), y0)
 
