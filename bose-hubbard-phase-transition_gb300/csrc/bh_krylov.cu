@@ -1432,8 +1432,8 @@ struct Launcher {
             // RB rows per thread: 4 on the FP32 vector path (2 with 40 or 48
             // outputs per pass, which keeps a restart's outputs in one pass), else 1
             constexpr int RB = (sizeof(T) == 4 && PV >= 1) ? 4 : 1;
-            constexpr int RB48 = (sizeof(T) == 4 && PV >= 1) ? 2 : 1;
             if constexpr (sizeof(T) == 4) {
+                constexpr int RB48 = PV >= 1 ? 2 : 1;
                 if (NO == 16) launch(k_rotate<T, 16, PV, RB>);
                 else if (NO == 24) launch(k_rotate<T, 24, PV, RB>);
                 else if (NO == 40) launch(k_rotate<T, 40, PV, RB48>);
