@@ -4,9 +4,12 @@ Maximilien-Hantonne/Bose-Hubbard-Phase-Transition exposes its exact path as
 C++ functions (``BH::fixed_set_basis``, ``BH::fixed_bosons_hamiltonian``,
 ``Neighbours``, ``Op::IRLM_eigen``, ``Analysis::gap_ratios``).  This module
 keeps those names, argument meanings and error behaviour and routes every
-computation through ``libbhgb300.so`` (include/bh_gb300.h): nothing here
-computes on the CPU except argument marshalling.  The library must load; if it
-is missing it is built, and if that fails the import fails loudly.
+computation of the exact path (basis, Hamiltonian, eigensolves, observables)
+through ``libbhgb300.so`` (include/bh_gb300.h): none of it runs on the CPU.
+The only host arithmetic is in small helpers of the reference's BH namespace
+that act on arrays the caller already holds (tags of a basis, the tag search,
+the mean-field single-site matrix).  The library must load; if it is missing
+it is built, and if that fails the import fails loudly.
 
 Layout conventions: a basis is returned as the reference returns it
 (tags[D], basis[m, D]); sparse matrices are scipy CSR in the reference's
@@ -15,6 +18,7 @@ column order; eigenvectors are columns.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 from dataclasses import dataclass
 
@@ -514,6 +518,45 @@ def spmm_tuning_reset():
 # BH namespace mirror (hamiltonian.hpp:33-112)
 # ---------------------------------------------------------------------------
 class BH:
+    # the primes table of the reference's tags (hamiltonian.cpp:144): site i
+    # weighs ln(PRIMES[i]), so tags order states like the integer prod p_i^n_i
+    PRIMES = (2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61, 67, 71, 73, 79,
+              83, 89, 97)
+
+    @staticmethod
+    def calculate_tag(basis: np.ndarray, primes, k: int) -> float:
+        """Tag of column k (hamiltonian.cpp:91-97): sum_i basis[i, k] ln(primes[i]),
+        summed over the sites in order."""
+        tag = 0.0
+        for i in range(basis.shape[0]):
+            tag += float(basis[i, k]) * math.log(float(primes[i]))
+        return tag
+
+    @staticmethod
+    def calculate_tags(basis: np.ndarray, primes) -> np.ndarray:
+        """Tags of every column (hamiltonian.cpp:100-106)."""
+        return np.array([BH.calculate_tag(basis, primes, k) for k in range(basis.shape[1])])
+
+    @staticmethod
+    def search_tag(tags: np.ndarray, x: float) -> int:
+        """Index of the tag closest to x (replaces hamiltonian.cpp:126-140, whose
+        binary search assumes sorted tags, which fixed_set_basis does not
+        produce; distinct states have tags far apart, so the closest tag is the
+        state's own for any order)."""
+        return int(np.argmin(np.abs(np.asarray(tags, np.float64) - x)))
+
+    @staticmethod
+    def h_MF(psi: float, p: int, mu: float, J: float, q: int) -> np.ndarray:
+        """Mean-field single-site Hamiltonian on occupations 0..2p
+        (hamiltonian.cpp:290-309), the same entries."""
+        k = 2 * p + 1
+        h = np.zeros((k, k))
+        for i in range(k):
+            h[i, i] = -mu * i + 0.5 * i * (i - 1) + q * J * psi * psi
+        for j in range(1, k):
+            h[j, j - 1] = h[j - 1, j] = -q * J * psi * math.sqrt(float(j))
+        return h
+
     @staticmethod
     def dimension(m: int, n: int) -> int:
         d = C.c_int64()
