@@ -546,6 +546,48 @@ class BH:
         return int(np.argmin(np.abs(np.asarray(tags, np.float64) - x)))
 
     @staticmethod
+    def sort_basis(tags: np.ndarray, basis: np.ndarray):
+        """The reference's sort_basis (hamiltonian.cpp:109-123): an argsort of the
+        tags followed by a cycle of swaps that applies the INVERSE of that
+        permutation, i.e. new column argsort[r] = old column r.  Returns new
+        (tags, basis); the tags of distinct states are distinct."""
+        tags = np.asarray(tags, np.float64)
+        perm = np.argsort(tags, kind="stable")
+        t = np.empty_like(tags)
+        t[perm] = tags
+        b = np.empty_like(basis)
+        b[:, perm] = basis
+        return t, b
+
+    @staticmethod
+    def max_set_basis(m: int, n: int):
+        """States with 1..n bosons (hamiltonian.cpp:151-165): the fixed-n bases
+        concatenated in increasing n, then sort_basis over all of them."""
+        tags = [np.zeros(0)]
+        basis = [np.zeros((m, 0))]
+        for bosons in range(1, n + 1):
+            t, b = BH.fixed_set_basis(m, bosons)
+            tags.append(t)
+            basis.append(b)
+        return BH.sort_basis(np.concatenate(tags), np.concatenate(basis, axis=1))
+
+    @staticmethod
+    def max_bosons_hamiltonian(neighbours, m: int, n_min: int, n_max: int, J: float, U: float,
+                               mu: float):
+        """Block-diagonal sum of the fixed-n Hamiltonians n_min..n_max
+        (hamiltonian.cpp:260-288; n_min clamped to 0, n_max to n_min), each one
+        term selected by fixed_bosons_hamiltonian as the reference selects it."""
+        import scipy.sparse as sp
+
+        n_min = max(0, n_min)
+        n_max = max(n_max, n_min)
+        blocks = []
+        for bosons in range(n_min, n_max + 1):
+            tags, basis = BH.fixed_set_basis(m, bosons)
+            blocks.append(BH.fixed_bosons_hamiltonian(neighbours, basis, tags, m, bosons, J, U, mu))
+        return sp.block_diag(blocks, format="csr")
+
+    @staticmethod
     def h_MF(psi: float, p: int, mu: float, J: float, q: int) -> np.ndarray:
         """Mean-field single-site Hamiltonian on occupations 0..2p
         (hamiltonian.cpp:290-309), the same entries."""

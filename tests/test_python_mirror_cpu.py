@@ -40,3 +40,77 @@ def test_h_mf_entries(pkg):
     h0 = BH.h_MF(0.0, p, 1.3, J, q)
     assert np.count_nonzero(h0 - np.diag(np.diag(h0))) == 0
     assert int(np.argmin(np.diag(h0))) == 2
+
+
+@pytest.mark.parametrize("key", ["3,3", "4,4", "2,3", "1,3"])
+def test_sort_basis_gives_the_reference_order(pkg, orc, golden, key):
+    # the reference's fixed_set_basis is init_lexicographic -> calculate_tags
+    # -> sort_basis; applied to the lexicographic basis, the mirror's
+    # sort_basis must give the golden order and tags bit for bit
+    rec = golden["basis"][key]
+    m, n = int(rec["m"]), int(rec["n"])
+    occ = orc.lex_states(m, n)
+    basis_lex = occ.T.astype(np.float64)
+    tags_lex = pkg.BH.calculate_tags(basis_lex, pkg.BH.PRIMES)
+    tags, basis = pkg.BH.sort_basis(tags_lex, basis_lex)
+    assert tags.tolist() == [float.fromhex(h) for h in rec["tags_hex"]]
+    col_of_lex = rec["col_of_lex"]
+    for r in range(occ.shape[0]):
+        assert np.array_equal(basis[:, col_of_lex[r]], basis_lex[:, r])
+
+
+def _fake_sectors(pkg, orc, monkeypatch, m, lists):
+    """fixed_set_basis / fixed_bosons_hamiltonian from the oracle (host only)."""
+    import scipy.sparse as sp
+
+    def fixed_set_basis(mm, n):
+        occ = orc.lex_states(mm, n)
+        b = occ.T.astype(np.float64)
+        return pkg.BH.sort_basis(pkg.BH.calculate_tags(b, pkg.BH.PRIMES), b)
+
+    def fixed_bosons_hamiltonian(nb, basis, tags, mm, n, J, U, mu):
+        from conftest import oracle_H
+
+        _, _, _, rp, ci, tv, vd = oracle_H(orc, mm, n, nb)
+        D = len(rp) - 1
+        if J != 0.0:
+            return sp.csr_matrix((J * tv, ci, rp), shape=(D, D))
+        return sp.diags(U * vd - mu * n).tocsr()
+
+    monkeypatch.setattr(pkg.BH, "fixed_set_basis", staticmethod(fixed_set_basis))
+    monkeypatch.setattr(pkg.BH, "fixed_bosons_hamiltonian", staticmethod(fixed_bosons_hamiltonian))
+
+
+def test_max_set_basis_holds_every_state_once(pkg, orc, monkeypatch):
+    from conftest import chain_lists
+
+    m, n = 4, 3
+    _fake_sectors(pkg, orc, monkeypatch, m, chain_lists(m))
+    tags, basis = pkg.BH.max_set_basis(m, n)
+    assert basis.shape == (m, sum(pkg.BH.dimension(m, k) for k in range(1, n + 1)))
+    seen = {tuple(basis[:, c].astype(int)) for c in range(basis.shape[1])}
+    assert len(seen) == basis.shape[1]
+    assert all(1 <= sum(s) <= n for s in seen)
+    # the reference's sort: column argsort(concatenated tags)[r] = concatenated column r
+    for c in range(basis.shape[1]):
+        assert tags[c] == pkg.BH.calculate_tag(basis, pkg.BH.PRIMES, c)
+
+
+def test_max_bosons_hamiltonian_blocks_and_clamping(pkg, orc, monkeypatch):
+    from conftest import chain_lists
+
+    m = 4
+    lists = chain_lists(m)
+    _fake_sectors(pkg, orc, monkeypatch, m, lists)
+    H = pkg.BH.max_bosons_hamiltonian(lists, m, -2, 3, 0.1, 0.0, 0.0)
+    dims = [pkg.BH.dimension(m, k) for k in range(0, 4)]
+    assert H.shape == (sum(dims), sum(dims))
+    o = 0
+    for k, d in enumerate(dims):
+        blk = pkg.BH.fixed_bosons_hamiltonian(lists, None, None, m, k, 0.1, 0.0, 0.0)
+        assert abs(H[o:o + d, o:o + d] - blk).max() == 0.0
+        assert H[o:o + d, o + d:].nnz == 0
+        o += d
+    # n_max < n_min: the single sector n_min
+    H1 = pkg.BH.max_bosons_hamiltonian(lists, m, 2, 1, 0.0, 1.0, 0.0)
+    assert H1.shape == (dims[2], dims[2])
