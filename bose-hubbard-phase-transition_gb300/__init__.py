@@ -673,6 +673,19 @@ class Op:
         order = np.argsort(-np.abs(ev), kind="stable")
         return ev[order].astype(complex), vec[order].T.astype(complex)
 
+    @staticmethod
+    def FOLM_eigen(O, nb_iter: int, **opt):
+        """Op::FOLM_eigen (operator.cpp:39-86) as intended: the lowest
+        min(nb_iter, n - 2, 32) eigenpairs of the symmetric O by a fully
+        re-orthogonalised Krylov method, real values ascending and the
+        eigenvectors as real columns (the reference's own FOLM is unfinished
+        and unused; this is the same solver as IRLM_eigen)."""
+        n = O.shape[0]
+        nev = max(1, min(int(nb_iter), n - 2, 32))
+        vals, vecs = Op.IRLM_eigen(O, nev, **opt)
+        order = np.argsort(vals.real, kind="stable")
+        return vals.real[order], np.ascontiguousarray(vecs.real[:, order])
+
 
 # ---------------------------------------------------------------------------
 # Analysis namespace mirror (analysis.hpp)

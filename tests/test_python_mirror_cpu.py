@@ -114,3 +114,26 @@ def test_max_bosons_hamiltonian_blocks_and_clamping(pkg, orc, monkeypatch):
     # n_max < n_min: the single sector n_min
     H1 = pkg.BH.max_bosons_hamiltonian(lists, m, 2, 1, 0.0, 1.0, 0.0)
     assert H1.shape == (dims[2], dims[2])
+
+
+def test_folm_eigen_clamps_and_orders(pkg, monkeypatch):
+    # the eigensolve itself is the GPU path of IRLM_eigen (tested with -m gpu);
+    # here a dense stand-in checks FOLM's count and ordering around it
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((12, 12))
+    A = A + A.T
+    w, z = np.linalg.eigh(A)
+    calls = []
+
+    def irlm(O, nev, **opt):
+        calls.append(nev)
+        order = np.argsort(-np.abs(w[:nev]), kind="stable")
+        return w[:nev][order].astype(complex), z[:, :nev][:, order].astype(complex)
+
+    monkeypatch.setattr(pkg.Op, "IRLM_eigen", staticmethod(irlm))
+    vals, vecs = pkg.Op.FOLM_eigen(A, 5)
+    assert calls[-1] == 5 and np.array_equal(vals, w[:5]) and np.array_equal(vecs, z[:, :5])
+    vals, _ = pkg.Op.FOLM_eigen(A, 50)
+    assert calls[-1] == 10 and np.array_equal(vals, w[:10])  # n - 2
+    pkg.Op.FOLM_eigen(A, 0)
+    assert calls[-1] == 1
