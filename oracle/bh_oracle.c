@@ -263,8 +263,22 @@ typedef struct {
     int n;
 } bho_op;
 
+/* Threads of the row loops inside one IRLM solve (0 = serial, the default).
+ * Row loops (the product, axpy-like updates, V Q) give the same bits with any
+ * thread count; inner products are then summed in fixed 8192-row chunks, so
+ * their value depends on neither the thread count nor the schedule, though it
+ * differs from the serial sum in the last bits.  Used by the timed CPU
+ * baseline, which must use every host core on a few large solves, the way the
+ * reference's grid loop would on many (src/analysis.cpp:302). */
+static int g_inner_threads = 0;
+
+void bho_set_inner_threads(int t) { g_inner_threads = t > 0 ? t : 0; }
+
+#define BHO_ROWS_PARALLEL _Pragma("omp parallel for schedule(static) num_threads(g_inner_threads) if (g_inner_threads > 1)")
+
 static void op_apply(const bho_op* A, const double* x, double* y) {
     const double sh = -A->mu * (double)A->n;
+    BHO_ROWS_PARALLEL
     for (int64_t r = 0; r < A->D; ++r) {
         double acc = 0.0;
         for (int64_t e = A->rp[r]; e < A->rp[r + 1]; ++e) acc += A->tv[e] * x[A->ci[e]];
@@ -429,9 +443,55 @@ void bho_start_vector(uint64_t seed, int64_t D, double* v) {
 }
 
 static double dotp(int64_t D, const double* a, const double* b) {
+    if (g_inner_threads > 1 && D > 65536) {
+        const int64_t CH = 8192;
+        int64_t nch = (D + CH - 1) / CH;
+        double* part = (double*)malloc(sizeof(double) * (size_t)nch);
+        BHO_ROWS_PARALLEL
+        for (int64_t c = 0; c < nch; ++c) {
+            int64_t e = (c + 1) * CH < D ? (c + 1) * CH : D;
+            double s = 0.0;
+            for (int64_t i = c * CH; i < e; ++i) s += a[i] * b[i];
+            part[c] = s;
+        }
+        double s = 0.0;
+        for (int64_t c = 0; c < nch; ++c) s += part[c];
+        free(part);
+        return s;
+    }
     double s = 0.0;
     for (int64_t i = 0; i < D; ++i) s += a[i] * b[i];
     return s;
+}
+
+/* out[j] = <V_j, w> for j < nc (V column-major, D x nc): dotp for each
+ * column, or with inner threads one pass over fixed 8192-row chunks whose
+ * partial sums are added in chunk order (the same value as dotp's chunked
+ * form, for any thread count). */
+static void gemv_t(int64_t D, const double* V, int nc, const double* w, double* out) {
+    if (!(g_inner_threads > 1 && D > 65536)) {
+        for (int j = 0; j < nc; ++j) out[j] = dotp(D, V + (size_t)j * D, w);
+        return;
+    }
+    const int64_t CH = 8192;
+    int64_t nch = (D + CH - 1) / CH;
+    double* part = (double*)malloc(sizeof(double) * (size_t)nch * (size_t)nc);
+    BHO_ROWS_PARALLEL
+    for (int64_t c = 0; c < nch; ++c) {
+        int64_t e = (c + 1) * CH < D ? (c + 1) * CH : D;
+        for (int j = 0; j < nc; ++j) {
+            const double* a = V + (size_t)j * D;
+            double s = 0.0;
+            for (int64_t i = c * CH; i < e; ++i) s += a[i] * w[i];
+            part[(size_t)c * nc + j] = s;
+        }
+    }
+    for (int j = 0; j < nc; ++j) {
+        double s = 0.0;
+        for (int64_t c = 0; c < nch; ++c) s += part[(size_t)c * nc + j];
+        out[j] = s;
+    }
+    free(part);
 }
 
 typedef struct {
@@ -482,12 +542,14 @@ static void factorize_from(arnoldi* ar, int from_k, int to_m) {
             restart = 1;
         }
         double* vi = ar->V + (size_t)i * D;
+        BHO_ROWS_PARALLEL
         for (int64_t r = 0; r < D; ++r) vi[r] = ar->f[r] / ar->beta;
         HH(i, i - 1) = restart ? 0.0 : ar->beta;
         op_apply(ar->A, vi, w);
         ar->nmatop++;
         int i1 = i + 1;
-        for (int j = 0; j < i1; ++j) h[j] = dotp(D, ar->V + (size_t)j * D, w);
+        gemv_t(D, ar->V, i1, w, h);
+        BHO_ROWS_PARALLEL
         for (int64_t r = 0; r < D; ++r) {
             double acc = w[r];
             for (int j = 0; j < i1; ++j) acc -= ar->V[(size_t)j * D + r] * h[j];
@@ -499,7 +561,7 @@ static void factorize_from(arnoldi* ar, int from_k, int to_m) {
             for (int j = 0; j < i1; ++j) HH(j, i) = h[j];
             continue;
         }
-        for (int j = 0; j < i1; ++j) vf[j] = dotp(D, ar->V + (size_t)j * D, ar->f);
+        gemv_t(D, ar->V, i1, ar->f, vf);
         double oe = 0.0;
         for (int j = 0; j < i1; ++j) oe = fmax(oe, fabs(vf[j]));
         int count = 0;
@@ -509,6 +571,7 @@ static void factorize_from(arnoldi* ar, int from_k, int to_m) {
                 ar->beta = 0.0;
                 break;
             }
+            BHO_ROWS_PARALLEL
             for (int64_t r = 0; r < D; ++r) {
                 double acc = ar->f[r];
                 for (int j = 0; j < i1; ++j) acc -= ar->V[(size_t)j * D + r] * vf[j];
@@ -516,7 +579,7 @@ static void factorize_from(arnoldi* ar, int from_k, int to_m) {
             }
             for (int j = 0; j < i1; ++j) h[j] += vf[j];
             ar->beta = sqrt(dotp(D, ar->f, ar->f));
-            for (int j = 0; j < i1; ++j) vf[j] = dotp(D, ar->V + (size_t)j * D, ar->f);
+            gemv_t(D, ar->V, i1, ar->f, vf);
             oe = 0.0;
             for (int j = 0; j < i1; ++j) oe = fmax(oe, fabs(vf[j]));
             ++count;
@@ -591,18 +654,25 @@ static void irlm_restart(arnoldi* ar, ritz* rz, int k) {
     for (int i = k; i < n; ++i) shifted_qr(ar, rz->val[i], Q);
     /* V <- V Q(:, 0:k), f <- V Q(:,k) H(k,k-1) + f Q(n-1,k-1) */
     double* Vn = (double*)malloc(sizeof(double) * (size_t)D * (size_t)(k + 1));
-    for (int j = 0; j <= k; ++j) {
-        double* out = Vn + (size_t)j * D;
-        for (int64_t r = 0; r < D; ++r) out[r] = 0.0;
-        for (int t = 0; t < n; ++t) {
-            double q = Q[(size_t)j * n + t];
-            if (q == 0.0) continue;
-            const double* vt = ar->V + (size_t)t * D;
-            for (int64_t r = 0; r < D; ++r) out[r] += q * vt[r];
+    /* per row, the same t-ascending accumulation as a column-by-column pass */
+    const int64_t RB = 4096;
+    BHO_ROWS_PARALLEL
+    for (int64_t r0 = 0; r0 < D; r0 += RB) {
+        int64_t r1 = r0 + RB < D ? r0 + RB : D;
+        for (int j = 0; j <= k; ++j) {
+            double* out = Vn + (size_t)j * D;
+            for (int64_t r = r0; r < r1; ++r) out[r] = 0.0;
+            for (int t = 0; t < n; ++t) {
+                double q = Q[(size_t)j * n + t];
+                if (q == 0.0) continue;
+                const double* vt = ar->V + (size_t)t * D;
+                for (int64_t r = r0; r < r1; ++r) out[r] += q * vt[r];
+            }
         }
     }
     double qf = Q[(size_t)(k - 1) * n + (n - 1)];
     double hk = HH(k, k - 1);
+    BHO_ROWS_PARALLEL
     for (int64_t r = 0; r < D; ++r) ar->f[r] = Vn[(size_t)k * D + r] * hk + ar->f[r] * qf;
     memcpy(ar->V, Vn, sizeof(double) * (size_t)D * (size_t)k);
     ar->beta = sqrt(dotp(D, ar->f, ar->f));

@@ -38,8 +38,12 @@ def build(force: bool = False) -> str:
     return LIB
 
 
-def build_ref(ref_root: str = "/root/reference") -> str | None:
-    """Compile the reference harness where the reference tree exists."""
+REFERENCE_TREE = os.environ.get("BH_REFERENCE_TREE", "/root/reference")
+
+
+def build_ref(ref_root: str = REFERENCE_TREE) -> str | None:
+    """Compile the reference harness where the reference tree exists
+    (BH_REFERENCE_TREE, default /root/reference)."""
     if not os.path.isdir(os.path.join(ref_root, "src")):
         return None
     if not os.path.exists(REF_LIB):
@@ -79,6 +83,7 @@ class Oracle:
             C.c_int, C.c_int, C.c_double, C.c_int, _f64p, _i32p,
         ]
         lib.bho_max_threads.restype = C.c_int
+        lib.bho_set_inner_threads.argtypes = [C.c_int]
         lib.bho_gap_ratio.restype = C.c_double
         lib.bho_gap_ratio.argtypes = [C.c_int, _f64p, C.c_void_p]
         lib.bho_spdm.argtypes = [C.c_int, C.c_int, C.c_int64, _u8p, _f64p, _f64p]
@@ -211,6 +216,10 @@ class Oracle:
 
     def max_threads(self) -> int:
         return int(self.lib.bho_max_threads())
+
+    def set_inner_threads(self, t: int):
+        """Threads of the row loops inside each IRLM solve (0 = serial)."""
+        self.lib.bho_set_inner_threads(int(t))
 
     # ---- observables ----
     def gap_ratio(self, evals):

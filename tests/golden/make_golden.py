@@ -13,7 +13,10 @@ oracle/Makefile into oracle/_ref/libbhref.so:
     neighbour slots and reads out of bounds);
   - Analysis::gap_ratios and Analysis::coherence;
   - Analysis::SCMF (analysis.cpp:111-178), the mean-field order parameter.
-Usage:  python tests/golden/make_golden.py [--quick | --scmf-only]
+Usage:  python tests/golden/make_golden.py [--quick | --scmf-only | --large]
+(--large writes reference_golden_large.json: basis orders at m=n=12, m=n=14
+and m=16, n=12, and the reference's IRLM at m=n=12; see large_cases).
+The reference tree is read from BH_REFERENCE_TREE (default /root/reference).
 """
 from __future__ import annotations
 
@@ -31,7 +34,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import oracle as orc  # noqa: E402
 
-REF_TREE = "/root/reference"
+REF_TREE = os.environ.get("BH_REFERENCE_TREE", "/root/reference")
 
 
 def hexs(a):
@@ -210,8 +213,76 @@ def update_scmf_only():
     print("wrote", path, os.path.getsize(path), "bytes")
 
 
+def large_cases():
+    """Golden values at the sizes of the large workloads, written to
+    reference_golden_large.json:
+      - the reference's own fixed_set_basis order at m=n=12, m=n=14 (76-bit
+        prime products) and m=16, n=12 (the 4x4 torus sector), checked here
+        state by state against the oracle's order and recorded as SHA-256 of
+        col_of_lex (int32 little-endian) and of the tags;
+      - the reference's Op::IRLM_eigen (Spectra, single thread) on the model
+        Hamiltonian at m=n=12, J=0.05, U=1, mu=0.6, nev=10, and with nev+2
+        (whose lowest 10 values are the lowest 10 with multiplicity).
+    The IRLM at D=1 352 078 takes about 15 minutes per run."""
+    orc.build()
+    if orc.build_ref(REF_TREE) is None:
+        raise SystemExit("reference tree not available")
+    o = orc.Oracle()
+    ref = orc.Reference()
+    out = {"generator": "tests/golden/make_golden.py --large",
+           "reference": "Maximilien-Hantonne/Bose-Hubbard-Phase-Transition"}
+    basis = {}
+    for m, n in [(12, 12), (14, 14), (16, 12)]:
+        t0 = time.time()
+        tags, rbasis = ref.fixed_set_basis(m, n)
+        occ = o.lex_states(m, n)
+        lex_ref = ref.init_lexicographic(m, n)
+        assert np.array_equal(lex_ref, occ.astype(np.float64)), (m, n, "lexicographic order")
+        del lex_ref
+        col_of_lex, lex_of_col = o.reference_order(occ)
+        assert np.array_equal(rbasis, occ[lex_of_col].astype(np.float64)), (m, n, "column order")
+        del rbasis
+        otags = o.tags(occ)
+        basis[f"{m},{n}"] = {
+            "m": m, "n": n, "D": int(len(tags)),
+            "col_of_lex_sha256": sha(col_of_lex.astype("<i4")),
+            "tags_sha256": sha(tags.astype("<f8")),
+            "oracle_tags_equal": bool(np.array_equal(otags[lex_of_col], tags)),
+            "first_cols_lex": lex_of_col[:16].tolist(),
+        }
+        print(f"basis {m},{n}: D={len(tags)} {time.time() - t0:.1f}s", flush=True)
+        del occ, tags
+    out["basis"] = basis
+
+    m, n, J, U, mu, nev = 12, 12, 0.05, 1.0, 0.6, 10
+    H = hamiltonian_ref_order(o, m, n, J, U, mu)
+
+    def run(k):
+        t0 = time.time()
+        re, im = ref.irlm(H, k)
+        return k, re, im, time.time() - t0
+
+    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+        res = {k: (re, im, dt) for k, re, im, dt in ex.map(run, [nev, nev + 2])}
+    re, im, dt = res[nev]
+    re2, _, dt2 = res[nev + 2]
+    out["irlm"] = {"m12n12": {
+        "m": m, "n": n, "J": J, "U": U, "mu": mu, "nev": nev, "converged": True,
+        "evals_reference_order": re.tolist(), "imag_max": float(np.abs(im).max()),
+        "evals_sorted": sorted(re.tolist()), "seconds": dt, "nnz": int(H.nnz),
+        "evals_lowest_from_nev_plus_2": sorted(re2.tolist())[:nev], "seconds_nev_plus_2": dt2,
+    }}
+    print(f"m12n12: {dt:.0f}s / {dt2:.0f}s E0={min(re)}", flush=True)
+    path = os.path.join(HERE, "reference_golden_large.json")
+    with open(path, "w") as f:
+        json.dump(out, f, indent=1)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
 if __name__ == "__main__":
     if "--scmf-only" in sys.argv:
         update_scmf_only()
+    elif "--large" in sys.argv:
+        large_cases()
     else:
         main("--quick" in sys.argv)
