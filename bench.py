@@ -116,12 +116,13 @@ def profile_traffic(kernel: str, algorithmic_bytes_per_launch: float | None = No
 class CpuReference:
     """The CPU restatement of the reference's path (oracle): Op::IRLM_eigen
     (Spectra GenEigsSolver, ncv = 2 nev + 1, SimpleRandom(0) start) on the
-    model Hamiltonian of each sector of the grid, FP64.  The five sector
-    Hamiltonians are built once (untimed).  Every solve uses all host cores
-    on its row loops (the product, the orthogonalisation, the restart
-    rotation): a single solve of the largest sector takes tens of seconds, so
-    the reference's OpenMP loop over grid points (analysis.cpp:302) could not
-    fill the cores within a bounded sample."""
+    model Hamiltonian of each sector of the grid, FP64, with the reference's
+    own parallelism -- OpenMP over grid points (analysis.cpp:302), one solve
+    per thread -- on every host core.  The five sector Hamiltonians are built
+    once (untimed).  A sample is one wave of concurrent solves of one sector:
+    as many points as there are cores, one thread each; in the sectors above
+    5 10^4 states a quarter as many points with four threads on each solve's
+    row loops (a wave of single-threaded solves there takes up to a minute)."""
 
     def __init__(self, threads: int = 0):
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -129,7 +130,6 @@ class CpuReference:
 
         self.orc = orc_mod.Oracle()
         self.threads = threads or (os.cpu_count() or 1)
-        self.orc.set_inner_threads(self.threads)
         off = np.zeros(M + 1, np.int32)
         flat = []
         for i in range(M):  # the periodic chain (Neighbours::chain_neighbours)
@@ -145,43 +145,69 @@ class CpuReference:
             rp, ci, tv = self.orc.build_T(occ, off, flat, lex_of_col, col_of_lex)
             self.ops[n] = (rp, ci, tv, self.orc.diag_V(occ, lex_of_col))
 
-    @staticmethod
-    def point(k: int):
-        """Sample k: sector SECTORS[k mod 5] at J index (7 + 13 k) mod 64, so
-        that consecutive samples cycle through the sectors and spread over J."""
-        return SECTORS[k % len(SECTORS)], (7 + 13 * k) % NJ
+    def shape(self, n: int):
+        """(concurrent solves, threads per solve) of a wave in sector n."""
+        inner = 4 if len(self.ops[n][3]) > 50000 and self.threads >= 8 else 1
+        return max(1, self.threads // inner), inner
 
-    def solve(self, k: int) -> float:
-        """Seconds of sample k's eigensolve."""
-        n, b = self.point(k)
+    def points(self, k: int):
+        """Wave k: sector SECTORS[k mod 5], J indices 8 + (7 + 13 i) mod 56 for
+        the wave's consecutive sample numbers i, so that waves spread over J.
+        The eight smallest J (b < 8, J < 0.042) are left out: there the
+        reference's IRLM (ncv = 21) does not reach 10 converged values within
+        its 1000 restarts at some points and would throw."""
+        n = SECTORS[k % len(SECTORS)]
+        groups, _ = self.shape(n)
+        return n, [8 + (7 + 13 * (k * 16 + i)) % (NJ - 8) for i in range(groups)]
+
+    def wave(self, k: int) -> tuple[int, int, float]:
+        """Runs wave k: (sector, solves, seconds)."""
+        n, bs = self.points(k)
+        groups, inner = self.shape(n)
         rp, ci, tv, vd = self.ops[n]
         t0 = time.perf_counter()
-        ev, nc = self.orc.irlm_batch(rp, ci, tv, vd, n, JS[b:b + 1], U, 0.0, nev=NEV, nthreads=1)
+        ev, nc = self.orc.irlm_wave(rp, ci, tv, vd, n, JS[bs], U, 0.0, nev=NEV, groups=groups, inner=inner)
         dt = time.perf_counter() - t0
-        if nc[0] < NEV:
-            raise RuntimeError(f"CPU reference did not converge (n={n}, J={JS[b]})")
-        return dt
+        if nc.min() < NEV:
+            raise RuntimeError(f"CPU reference did not converge (n={n})")
+        return n, len(bs), dt
 
     @staticmethod
-    def rate(times: dict) -> float:
+    def rate(per_solve: dict) -> float:
         """Eigensolves/s of the full grid (equal numbers of points in every
-        sector) from the mean solve time of each sector."""
-        return len(SECTORS) / sum(float(np.mean(times[n])) for n in SECTORS)
+        sector) from each sector's seconds per solve (wave time / solves)."""
+        return len(SECTORS) / sum(float(np.mean(per_solve[n])) for n in SECTORS)
 
 
 def cpu_sample_rate():
-    """One cycle of five samples (one J point per sector): (rate, cores, seconds)."""
+    """One cycle of five waves (one per sector): (rate, cores, seconds)."""
     ref = CpuReference()
-    times = {}
+    per_solve, tot = {}, 0.0
     for k in range(len(SECTORS)):
-        times.setdefault(ref.point(k)[0], []).append(ref.solve(k))
-    return ref.rate(times), ref.threads, sum(sum(v) for v in times.values())
+        n, cnt, dt = ref.wave(k)
+        per_solve.setdefault(n, []).append(dt / cnt)
+        tot += dt
+    return ref.rate(per_solve), ref.threads, tot
 
 
-CPU_SAMPLE = ("one J point per sector per cycle (J index (7 + 13 k) mod 64 for sample k), the five "
-              "sectors in turn; rate = 5 / (sum over sectors of the mean seconds per solve), i.e. the "
-              "full grid's eigensolves/s with every sector weighted as in the grid; FP64 restatement "
-              "of Op::IRLM_eigen (Spectra GenEigsSolver, ncv=2nev+1) with its row loops on all host cores")
+def cpu_sample_rate_subprocess():
+    """cpu_sample_rate in a fresh process: in the GPU arm's process (CUDA
+    runtime and solver host threads alive) the same waves ran 2.6x slower."""
+    r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-sample"],
+                       capture_output=True, text=True, timeout=900)
+    if r.returncode != 0:
+        raise RuntimeError("CPU sample failed: " + r.stderr[-2000:])
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    return d["rate"], d["cores"], d["seconds"]
+
+
+CPU_SAMPLE = ("waves of concurrent solves, one sector per wave, the five sectors in turn: per wave one "
+              "solve per host core (sectors n=8,9) or a quarter as many with four threads on each solve's "
+              "row loops (n=10..12, above 5e4 states); J indices 8 + (7 + 13 i) mod 56 (the reference's "
+              "IRLM fails to converge at some of the eight smallest J); rate = 5 / (sum over sectors of "
+              "wave seconds / solves in the wave), i.e. the full grid's eigensolves/s with every sector "
+              "weighted as in the grid; FP64 restatement of Op::IRLM_eigen (Spectra GenEigsSolver, "
+              "ncv=2nev+1), OpenMP over points as analysis.cpp:302")
 
 
 # ---------------------------------------------------------------------------
@@ -410,9 +436,9 @@ def run_ours(args):
                 "non_default_shape": int(sum(e["shape"] != pkg.spmm_candidates(e["ncols"], e["matrix_free"])[0]
                                              for e in tuned))}
 
-        rate, cores, secs = cpu_sample_rate()
+        rate, cores, secs = cpu_sample_rate_subprocess()
         out["cpu_baseline"] = {"value": round(rate, 4), "unit": "eigensolves/s", "cores": cores,
-                               "kind": "port", "sample": "one cycle: " + CPU_SAMPLE,
+                               "kind": "port", "sample": "one cycle of five waves: " + CPU_SAMPLE,
                                "seconds": round(secs, 2), "cpu": cpu_model()}
         print(json.dumps(out), flush=True)
     if ws > 1:
@@ -437,21 +463,23 @@ def cpu_model() -> str:
 
 
 def run_reference(args):
-    """One step = one sample of CpuReference (one J point of one sector, the
-    sectors in turn); value = the full grid's eigensolves/s from the mean solve
-    time of every sector (CpuReference.rate).  Only rank 0 runs."""
+    """One step = one wave of CpuReference (one sector, the sectors in turn);
+    value = the full grid's eigensolves/s from every sector's seconds per
+    solve (CpuReference.rate).  Only rank 0 runs."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     ref = CpuReference()
     for k in range(args.warmup):
-        ref.solve(k)
-    times = {}
+        ref.wave(k)
+    per_solve, tot, solves = {}, 0.0, 0
     steps = max(args.steps, len(SECTORS))  # every sector at least once
     for k in range(args.warmup, args.warmup + steps):
-        times.setdefault(ref.point(k)[0], []).append(ref.solve(k))
-    tot = sum(sum(v) for v in times.values())
-    value = ref.rate(times)
+        n, cnt, dt = ref.wave(k)
+        per_solve.setdefault(n, []).append(dt / cnt)
+        tot += dt
+        solves += cnt
+    value = ref.rate(per_solve)
     out = {"impl": "reference", "metric": METRIC,
            "value": round(value, 4), "unit": "eigensolves/s", "n_gpus": ws, "steps": steps,
            "warmup": args.warmup, "ms_per_step": round(1e3 * tot / steps, 3),
@@ -459,8 +487,9 @@ def run_reference(args):
            "data": "synthetic (Hamiltonian determined by m, n, J, U; seeded start vector)",
            "config": workload_config(ws),
            "cpu_baseline": {"value": round(value, 4), "unit": "eigensolves/s", "cores": ref.threads,
-                            "kind": "port", "sample": "one sample per step: " + CPU_SAMPLE,
-                            "seconds_per_sector": {str(n): round(float(np.mean(v)), 3) for n, v in times.items()},
+                            "kind": "port", "sample": "one wave per step: " + CPU_SAMPLE,
+                            "solves": solves,
+                            "seconds_per_solve": {str(n): round(float(np.mean(v)), 3) for n, v in per_solve.items()},
                             "cpu": cpu_model()},
            "e2e": {"value": round(value, 4), "unit": "eigensolves/s",
                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -681,6 +710,10 @@ def run_mean_field(args, pkg, torch):
 
 
 def main():
+    if "--cpu-sample" in sys.argv:
+        rate, cores, secs = cpu_sample_rate()
+        print(json.dumps({"rate": rate, "cores": cores, "seconds": secs}), flush=True)
+        return
     args = parse()
     if args.workload != "batched":
         if args.impl == "reference":

@@ -274,11 +274,11 @@ static int g_inner_threads = 0;
 
 void bho_set_inner_threads(int t) { g_inner_threads = t > 0 ? t : 0; }
 
-#define BHO_ROWS_PARALLEL _Pragma("omp parallel for schedule(static) num_threads(g_inner_threads) if (g_inner_threads > 1)")
+#define BHO_ROWS_PARALLEL _Pragma("omp parallel for schedule(static) num_threads(g_inner_threads) if (g_inner_threads > 1 && D > 65536)")
 
 static void op_apply(const bho_op* A, const double* x, double* y) {
     const double sh = -A->mu * (double)A->n;
-    BHO_ROWS_PARALLEL
+#pragma omp parallel for schedule(static) num_threads(g_inner_threads) if (g_inner_threads > 1 && A->D > 65536)
     for (int64_t r = 0; r < A->D; ++r) {
         double acc = 0.0;
         for (int64_t e = A->rp[r]; e < A->rp[r + 1]; ++e) acc += A->tv[e] * x[A->ci[e]];
@@ -816,6 +816,29 @@ int bho_irlm_batch(int64_t D, const int64_t* rp, const int32_t* ci, const double
                                 evals + (size_t)s * nev, NULL, NULL, NULL);
     }
     (void)nthreads;
+    return 0;
+}
+
+/* One wave of the reference's grid loop (src/analysis.cpp:302): nsolve
+ * independent IRLM solves of one operator run `groups` at a time (OpenMP,
+ * dynamic schedule), each solve's row loops on `inner` threads (nested
+ * parallelism; inner = 1 is the reference's own one-solve-per-thread form).
+ * evals nsolve x nev (reference order), nconv_out per solve. */
+int bho_irlm_wave(int64_t D, const int64_t* rp, const int32_t* ci, const double* tv,
+                  const double* vd, int n_bosons, int nsolve, const double* J,
+                  const double* U, const double* mu, int nev, int maxit, double tol,
+                  int groups, int inner, double* evals, int* nconv_out) {
+    const int saved = g_inner_threads;
+    g_inner_threads = inner > 1 ? inner : 0;
+#ifdef _OPENMP
+    if (inner > 1) omp_set_max_active_levels(2);
+#pragma omp parallel for schedule(dynamic) num_threads(groups > 0 ? groups : 1)
+#endif
+    for (int s = 0; s < nsolve; ++s) {
+        nconv_out[s] = bho_irlm(D, rp, ci, tv, vd, n_bosons, J[s], U[s], mu[s], nev, maxit, tol,
+                                evals + (size_t)s * nev, NULL, NULL, NULL);
+    }
+    g_inner_threads = saved;
     return 0;
 }
 

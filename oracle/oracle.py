@@ -84,6 +84,10 @@ class Oracle:
         ]
         lib.bho_max_threads.restype = C.c_int
         lib.bho_set_inner_threads.argtypes = [C.c_int]
+        lib.bho_irlm_wave.argtypes = [
+            C.c_int64, _i64p, _i32p, _f64p, _f64p, C.c_int, C.c_int, _f64p, _f64p, _f64p,
+            C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, _f64p, _i32p,
+        ]
         lib.bho_gap_ratio.restype = C.c_double
         lib.bho_gap_ratio.argtypes = [C.c_int, _f64p, C.c_void_p]
         lib.bho_spdm.argtypes = [C.c_int, C.c_int, C.c_int64, _u8p, _f64p, _f64p]
@@ -212,6 +216,19 @@ class Oracle:
         nc = np.zeros(S, np.int32)
         self.lib.bho_irlm_batch(len(vd), rp, ci, tv, vd, n, S, J, U, mu, nev, maxit, tol,
                                 nthreads, ev, nc)
+        return ev, nc
+
+    def irlm_wave(self, rp, ci, tv, vd, n, J, U, mu, nev=10, maxit=1000, tol=1e-10,
+                  groups=1, inner=1):
+        """Independent solves, `groups` at a time, each on `inner` threads."""
+        J = np.ascontiguousarray(J, np.float64)
+        S = len(J)
+        U = np.ascontiguousarray(np.broadcast_to(U, (S,)), np.float64)
+        mu = np.ascontiguousarray(np.broadcast_to(mu, (S,)), np.float64)
+        ev = np.zeros((S, nev))
+        nc = np.zeros(S, np.int32)
+        self.lib.bho_irlm_wave(len(vd), rp, ci, tv, vd, n, S, J, U, mu, nev, maxit, tol,
+                               groups, inner, ev, nc)
         return ev, nc
 
     def max_threads(self) -> int:
