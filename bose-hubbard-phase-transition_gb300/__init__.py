@@ -73,7 +73,7 @@ EXPORTS = [
     "bh_hamiltonian_create_matrix_free", "bh_hamiltonian_is_matrix_free",
     "bh_hamiltonian_destroy", "bh_hamiltonian_nnz", "bh_hamiltonian_csr",
     "bh_hamiltonian_apply", "bh_hamiltonian_apply_noalloc", "bh_solver_opts_default", "bh_eigsh", "bh_eigsh_csr",
-    "bh_eigsh_batch", "bh_eigsh_batch_vectors", "bh_eigsh_batch_sectors", "bh_dense_eigh", "bh_gap_ratios", "bh_spdm", "bh_phase_map", "bh_scmf", "bh_mean_field_grid", "bh_profile_enable",
+    "bh_eigsh_batch", "bh_eigsh_batch_status", "bh_eigsh_batch_vectors", "bh_eigsh_batch_sectors", "bh_dense_eigh", "bh_gap_ratios", "bh_spdm", "bh_phase_map", "bh_scmf", "bh_mean_field_grid", "bh_profile_enable",
     "bh_profile_reset", "bh_profile_count", "bh_profile_get",
     "bh_spmm_candidates", "bh_hamiltonian_apply_shape", "bh_spmm_autotune", "bh_spmm_tuning_count",
     "bh_spmm_tuning_get", "bh_spmm_tuning_reset",
@@ -121,6 +121,8 @@ def load() -> C.CDLL:
                                C.POINTER(bh_solve_info)]
     L.bh_eigsh_batch.argtypes = [vp, C.c_int, vp, vp, vp, C.POINTER(bh_solver_opts), vp, vp, vp,
                                  C.POINTER(bh_solve_info)]
+    L.bh_eigsh_batch_status.argtypes = [vp, C.c_int, vp, vp, vp, C.POINTER(bh_solver_opts), vp, vp, vp,
+                                        vp, C.POINTER(bh_solve_info)]
     L.bh_eigsh_batch_vectors.argtypes = [vp, C.c_int, vp, vp, vp, C.POINTER(bh_solver_opts), vp, vp, vp,
                                          vp, C.POINTER(bh_solve_info)]
     L.bh_eigsh_batch_sectors.argtypes = [C.c_int, vp, C.c_int, vp, vp, vp, C.POINTER(bh_solver_opts), vp, vp, vp,
@@ -336,10 +338,12 @@ class Hamiltonian:
                                C.byref(info)))
         return ev, rs, (None if vec is None else vec.T.copy()), _info(info)
 
-    def eigsh_batch(self, J, U, mu, nev: int = 10, vectors: bool = False, **opt):
+    def eigsh_batch(self, J, U, mu, nev: int = 10, vectors: bool = False, status: bool = False, **opt):
         """Batched lowest eigenpairs of (J[s], U[s], mu[s]).  Returns
         ev, resid [S, nev], nconv [S], info, and with vectors=True also the
-        eigenvectors [S, nev, D] (rows in opt['order'], reference by default)."""
+        eigenvectors [S, nev, D] (rows in opt['order'], reference by default);
+        with status=True (not with vectors) a per-point status array [S]
+        (BH_OK, BH_ERR_NOCONV or BH_ERR_BREAKDOWN) instead."""
         J = np.ascontiguousarray(J, np.float64)
         S = len(J)
         U = np.ascontiguousarray(np.broadcast_to(U, (S,)), np.float64)
@@ -349,6 +353,13 @@ class Hamiltonian:
         rs = np.zeros((S, nev))
         nc = np.zeros(S, np.int32)
         info = bh_solve_info()
+        if status:
+            if vectors:
+                raise ValueError("status=True is not available with vectors=True")
+            st = np.zeros(S, np.int32)
+            _check(load().bh_eigsh_batch_status(self._h, S, _ptr(J), _ptr(U), _ptr(mu), C.byref(o),
+                                                _ptr(ev), _ptr(rs), _ptr(nc), _ptr(st), C.byref(info)))
+            return ev, rs, nc, _info(info), st
         if vectors:
             vec = np.zeros((S, nev, self.D))
             _check(load().bh_eigsh_batch_vectors(self._h, S, _ptr(J), _ptr(U), _ptr(mu), C.byref(o),
@@ -735,7 +746,7 @@ class Analysis:
     @staticmethod
     def exact_parameters(m: int, n: int, J: float, U: float, mu: float, s: float, r: float,
                          fixed_param: str, path: str | None = "phase.txt", nb_eigen: int = 20,
-                         precision: int = PREC_MIXED, max_batch: int = 128):
+                         precision: int = PREC_FP64, max_batch: int = 128):
         """Analysis::exact_parameters + calculate_and_save (analysis.cpp:207-427)
         on the device: the 1D periodic chain of m sites with n bosons; one of
         J, U, mu fixed ("J", "U", anything else = mu) and the other two swept

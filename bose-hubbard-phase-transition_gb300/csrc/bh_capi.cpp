@@ -47,6 +47,22 @@ static void check_solver_opts(const bh_solver_opts* o) {
     BH_REQUIRE(o->precision == BH_PREC_FP64 || o->precision == BH_PREC_MIXED, "unknown precision mode");
     BH_REQUIRE(o->order == BH_ORDER_REFERENCE || o->order == BH_ORDER_LEX, "unknown vector order");
     BH_REQUIRE(o->nev >= 1, "nb_eigen must be >= 1");
+    BH_REQUIRE(std::isfinite(o->tol) && o->tol >= 0.0, "tol must be finite and >= 0");
+}
+
+// Hamiltonian parameters (and any other real inputs) must be finite: a NaN or
+// an infinity would run a whole solve on garbage, so it is rejected before
+// any device work.
+static void require_finite(const double* v, int64_t n, const char* what) {
+    for (int64_t i = 0; i < n; ++i)
+        if (!std::isfinite(v[i])) throw Error(BH_ERR_ARG, std::string(what) + " must be finite (entry " +
+                                                              std::to_string(i) + " is not)");
+}
+
+static void require_finite_params(double J, double U, double mu) {
+    BH_REQUIRE(std::isfinite(J), "J must be finite");
+    BH_REQUIRE(std::isfinite(U), "U must be finite");
+    BH_REQUIRE(std::isfinite(mu), "mu must be finite");
 }
 
 // fills the geometry of a request from the options and the dimension
@@ -77,6 +93,14 @@ static SolveRequest make_request(const bh_solver_opts* o, int64_t D, int S) {
     rq.seed = o->seed;
     rq.want_vectors = o->want_vectors != 0;
     return rq;
+}
+
+// single-point calls: the reference throws when the solve fails (operator.cpp:27-29)
+static void throw_if_failed(const SolveResult& r, int nev) {
+    if (r.status[0] == BH_ERR_BREAKDOWN)
+        throw Error(BH_ERR_BREAKDOWN, "Krylov space exhausted before nb_eigen eigenvalues "
+                                      "(invariant start block, or fewer states than requested)");
+    if (r.nconv[0] < nev) throw Error(BH_ERR_NOCONV, "Eigenvalue computation failed.");
 }
 
 static void fill_info(bh_solve_info* info, const SolveResult& r, int nev, double secs) {
@@ -292,6 +316,7 @@ int bh_hamiltonian_csr(const bh_hamiltonian* h, int order, double J, double U, d
     return guard([&] {
         BH_REQUIRE(h != nullptr && row_ptr && col && val, "null argument");
         BH_REQUIRE(order == BH_ORDER_REFERENCE || order == BH_ORDER_LEX, "unknown order");
+        require_finite_params(J, U, mu);
         const int64_t D = h->D, nz = h->nnz + D;
         Stream st;
         DevBuf<int64_t> rp(D + 1);
@@ -311,6 +336,7 @@ int bh_hamiltonian_apply(const bh_hamiltonian* h, int order, double J, double U,
                          int nvec, const double* x, double* y) {
     return guard([&] {
         BH_REQUIRE(h != nullptr && x && y && nvec >= 1, "null argument");
+        require_finite_params(J, U, mu);
         const int64_t D = h->D;
         Stream st;
         DevBuf<double> dx(D * nvec), dy(D * nvec), tmp(D * nvec), prm(3);
@@ -353,28 +379,48 @@ static void write_vectors(const bh_hamiltonian* h, const SolveResult& r, int S, 
         for (int64_t rr = 0; rr < D; ++rr) evecs[(size_t)k * D + col[rr]] = r.vecs[(size_t)k * D + rr];
 }
 
+static void batch_solve(const bh_hamiltonian* h, int nsolve, const double* J, const double* U,
+                        const double* mu, const bh_solver_opts* o, double* evals, double* resid,
+                        int* nconv, int* status, double* evecs, bh_solve_info* info) {
+    const auto t0 = std::chrono::steady_clock::now();
+    BH_REQUIRE(h != nullptr && J && U && mu && evals, "null argument");
+    BH_REQUIRE(nsolve >= 1, "nsolve must be >= 1");
+    check_solver_opts(o);
+    require_finite(J, nsolve, "J");
+    require_finite(U, nsolve, "U");
+    require_finite(mu, nsolve, "mu");
+    SolveRequest rq = make_request(o, h->D, nsolve);
+    rq.want_vectors = evecs != nullptr;
+    rq.d_perm = h->basis->d_col_of_lex.p;
+    rq.J.assign(J, J + nsolve);
+    rq.U.assign(U, U + nsolve);
+    rq.shift.resize(nsolve);
+    for (int s = 0; s < nsolve; ++s) rq.shift[s] = -mu[s] * (double)h->n;
+    Stream st;
+    SolveResult r = block_lanczos(op64_of(h), op32_of(h), rq, st);
+    std::memcpy(evals, r.evals.data(), r.evals.size() * sizeof(double));
+    if (resid) std::memcpy(resid, r.resid.data(), r.resid.size() * sizeof(double));
+    if (nconv) std::memcpy(nconv, r.nconv.data(), nsolve * sizeof(int));
+    if (status)
+        for (int s = 0; s < nsolve; ++s)
+            status[s] = r.status[s] != BH_OK ? r.status[s] : (r.nconv[s] < o->nev ? BH_ERR_NOCONV : BH_OK);
+    if (evecs) write_vectors(h, r, nsolve, o->nev, o->order, evecs);
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    fill_info(info, r, o->nev, secs);
+}
+
 int bh_eigsh_batch(const bh_hamiltonian* h, int nsolve, const double* J, const double* U,
                    const double* mu, const bh_solver_opts* o, double* evals, double* resid,
                    int* nconv, bh_solve_info* info) {
+    return guard([&] { batch_solve(h, nsolve, J, U, mu, o, evals, resid, nconv, nullptr, nullptr, info); });
+}
+
+int bh_eigsh_batch_status(const bh_hamiltonian* h, int nsolve, const double* J, const double* U,
+                          const double* mu, const bh_solver_opts* o, double* evals, double* resid,
+                          int* nconv, int* status, bh_solve_info* info) {
     return guard([&] {
-        const auto t0 = std::chrono::steady_clock::now();
-        BH_REQUIRE(h != nullptr && J && U && mu && evals, "null argument");
-        BH_REQUIRE(nsolve >= 1, "nsolve must be >= 1");
-        check_solver_opts(o);
-        SolveRequest rq = make_request(o, h->D, nsolve);
-        rq.want_vectors = false;
-        rq.d_perm = h->basis->d_col_of_lex.p;
-        rq.J.assign(J, J + nsolve);
-        rq.U.assign(U, U + nsolve);
-        rq.shift.resize(nsolve);
-        for (int s = 0; s < nsolve; ++s) rq.shift[s] = -mu[s] * (double)h->n;
-        Stream st;
-        SolveResult r = block_lanczos(op64_of(h), op32_of(h), rq, st);
-        std::memcpy(evals, r.evals.data(), r.evals.size() * sizeof(double));
-        if (resid) std::memcpy(resid, r.resid.data(), r.resid.size() * sizeof(double));
-        if (nconv) std::memcpy(nconv, r.nconv.data(), nsolve * sizeof(int));
-        const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-        fill_info(info, r, o->nev, secs);
+        BH_REQUIRE(status != nullptr, "null argument");
+        batch_solve(h, nsolve, J, U, mu, o, evals, resid, nconv, status, nullptr, info);
     });
 }
 
@@ -382,25 +428,8 @@ int bh_eigsh_batch_vectors(const bh_hamiltonian* h, int nsolve, const double* J,
                            const double* mu, const bh_solver_opts* o, double* evals, double* resid,
                            int* nconv, double* evecs, bh_solve_info* info) {
     return guard([&] {
-        const auto t0 = std::chrono::steady_clock::now();
-        BH_REQUIRE(h != nullptr && J && U && mu && evals && evecs, "null argument");
-        BH_REQUIRE(nsolve >= 1, "nsolve must be >= 1");
-        check_solver_opts(o);
-        SolveRequest rq = make_request(o, h->D, nsolve);
-        rq.want_vectors = true;
-        rq.d_perm = h->basis->d_col_of_lex.p;
-        rq.J.assign(J, J + nsolve);
-        rq.U.assign(U, U + nsolve);
-        rq.shift.resize(nsolve);
-        for (int s = 0; s < nsolve; ++s) rq.shift[s] = -mu[s] * (double)h->n;
-        Stream st;
-        SolveResult r = block_lanczos(op64_of(h), op32_of(h), rq, st);
-        std::memcpy(evals, r.evals.data(), r.evals.size() * sizeof(double));
-        if (resid) std::memcpy(resid, r.resid.data(), r.resid.size() * sizeof(double));
-        if (nconv) std::memcpy(nconv, r.nconv.data(), nsolve * sizeof(int));
-        write_vectors(h, r, nsolve, o->nev, o->order, evecs);
-        const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-        fill_info(info, r, o->nev, secs);
+        BH_REQUIRE(evecs != nullptr, "null argument");
+        batch_solve(h, nsolve, J, U, mu, o, evals, resid, nconv, nullptr, evecs, info);
     });
 }
 
@@ -412,6 +441,9 @@ int bh_eigsh_batch_sectors(int nh, const bh_hamiltonian* const* hs, int nsolve, 
         BH_REQUIRE(nh >= 1 && hs && J && U && mu && evals, "null argument or nh < 1");
         BH_REQUIRE(nsolve >= 1, "nsolve must be >= 1");
         check_solver_opts(o);
+        require_finite(J, nsolve, "J");
+        require_finite(U, nsolve, "U");
+        require_finite(mu, nsolve, "mu");
         for (int k = 0; k < nh; ++k) BH_REQUIRE(hs[k] != nullptr, "null Hamiltonian");
         int dev = 0;
         BH_CUDA(cudaGetDevice(&dev));
@@ -478,6 +510,7 @@ int bh_eigsh(const bh_hamiltonian* h, double J, double U, double mu, const bh_so
         const auto t0 = std::chrono::steady_clock::now();
         BH_REQUIRE(h != nullptr && evals, "null argument");
         check_solver_opts(o);
+        require_finite_params(J, U, mu);
         SolveRequest rq = make_request(o, h->D, 1);
         rq.want_vectors = evecs != nullptr;
         rq.d_perm = h->basis->d_col_of_lex.p;
@@ -491,7 +524,7 @@ int bh_eigsh(const bh_hamiltonian* h, double J, double U, double mu, const bh_so
         write_vectors(h, r, 1, o->nev, o->order, evecs);
         const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         fill_info(info, r, o->nev, secs);
-        if (r.nconv[0] < o->nev) throw Error(BH_ERR_NOCONV, "Eigenvalue computation failed.");
+        throw_if_failed(r, o->nev);
     });
 }
 
@@ -507,6 +540,7 @@ int bh_eigsh_csr(int64_t dim, const int64_t* row_ptr, const int32_t* col, const 
         const int64_t nnz = row_ptr[dim];
         for (int64_t r = 0; r < dim; ++r) BH_REQUIRE(row_ptr[r + 1] >= row_ptr[r], "row_ptr must be non-decreasing");
         for (int64_t e = 0; e < nnz; ++e) BH_REQUIRE(col[e] >= 0 && col[e] < dim, "column index out of range");
+        require_finite(val, nnz, "matrix values");
         Stream st;
         DevBuf<int64_t> rp(dim + 1);
         DevBuf<int32_t> ci(nnz);
@@ -547,7 +581,7 @@ int bh_eigsh_csr(int64_t dim, const int64_t* row_ptr, const int32_t* col, const 
         if (evecs) std::memcpy(evecs, r.vecs.data(), (size_t)o->nev * dim * sizeof(double));
         const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         fill_info(info, r, o->nev, secs);
-        if (r.nconv[0] < o->nev) throw Error(BH_ERR_NOCONV, "Eigenvalue computation failed.");
+        throw_if_failed(r, o->nev);
     });
 }
 
@@ -599,6 +633,8 @@ int bh_phase_map(int m, int n_lo, int nsec, int nJ, const double* e0, int nmu, c
     return guard([&] {
         BH_REQUIRE(m >= 1 && nsec >= 1 && nJ >= 1 && nmu >= 1, "empty grid");
         BH_REQUIRE(e0 && mu && density && compressibility, "null argument");
+        require_finite(e0, (int64_t)nsec * nJ, "e0");
+        require_finite(mu, nmu, "mu");
         Stream st;
         DevBuf<double> de((size_t)nsec * nJ), dm(nmu), dd((size_t)nJ * nmu), dk((size_t)nJ * nmu);
         BH_CUDA(cudaMemcpyAsync(de.p, e0, (size_t)nsec * nJ * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -644,6 +680,7 @@ int bh_hamiltonian_apply_shape(const bh_hamiltonian* h, int precision, double J,
     return guard([&] {
         BH_REQUIRE(h != nullptr && x && y && nvec >= 1, "null argument");
         BH_REQUIRE(precision == BH_PREC_FP64 || precision == BH_PREC_MIXED, "unknown precision mode");
+        require_finite_params(J, U, mu);
         const SpmmShape s = shape ? shape_in(*shape) : spmm_resolve(SpmmChoice{}, nvec, h->matrix_free);
         BH_REQUIRE(spmm_shape_valid(s, nvec, h->matrix_free),
                    "launch shape: lanes must be a power of two <= 32 dividing nvec (32 at any nvec "

@@ -79,7 +79,8 @@ struct Stream {
     operator cudaStream_t() const { return s; }
 };
 
-int sm_count();
+constexpr int kMaxDevices = 64;  // device ordinals with cached attributes
+int sm_count();                  // multiprocessors of the current device
 
 // ---------------------------------------------------------------------------
 // Fock basis.  States are identified by their lexicographic index r (the

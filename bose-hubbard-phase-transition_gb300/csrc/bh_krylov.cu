@@ -28,10 +28,12 @@
 // vectors (FP64 SpMM, FP64 Gram matrices, FP64 generalised eigensolve) gives
 // the returned eigenvalues and their true FP64 residuals.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <limits>
 #include <numeric>
 #include <thread>
 #include <type_traits>
@@ -1048,26 +1050,41 @@ __global__ void k_convert(int64_t n, const A* __restrict__ in, B* __restrict__ o
         out[i] = (B)in[i];
 }
 
-// ||(Y - theta_i X) z_i||^2 partials for column t = s K + i (FP64)
+// Combination of Ritz-type columns (FP64), column t = s K + i of a group:
+//   v = sum_a (Y1 - theta_t X1)[r][s K + a] Z1_s[a][i] + sum_a (Y2 - theta_t X2)[r][s K + a] Z2_s[a][i]
+// (X1, X2 may be null: no theta term; Y2 null: no second sum), written to
+// out[r][t] (if not null) and/or summed as |v|^2 over a chunk of rows into
+// part[chunk][t] (if not null).  Z_s[a][i] at Z + (s K + a) K + i.
 __global__ void __launch_bounds__(512)
-k_resid(int64_t D, int ncols, int ld, int K, const double* __restrict__ X, const double* __restrict__ Y,
-        const double* __restrict__ theta, const double* __restrict__ Z, int64_t rows_per_chunk,
-        double* __restrict__ part) {
+k_ritz_mix(int64_t D, int ncols, int ld, int K, const double* __restrict__ Y1, const double* __restrict__ X1,
+           const double* __restrict__ Z1, const double* __restrict__ Y2, const double* __restrict__ X2,
+           const double* __restrict__ Z2, const double* __restrict__ theta, double* __restrict__ out,
+           int64_t rows_per_chunk, double* __restrict__ part) {
     extern __shared__ double s_red2[];
     const int t = threadIdx.x % ncols, ro = threadIdx.x / ncols, R = blockDim.x / ncols;
     const int s = t / K, i = t % K;
-    const double th = theta[t];
-    const double* z = Z + (size_t)s * K * K;  // z[a * K + i]
+    const double th = theta ? theta[t] : 0.0;
+    const double* z1 = Z1 + (size_t)s * K * K;
+    const double* z2 = Z2 ? Z2 + (size_t)s * K * K : nullptr;
     const int64_t r0 = (int64_t)blockIdx.x * rows_per_chunk;
     const int64_t r1 = min(D, r0 + rows_per_chunk);
     double acc = 0.0;
     for (int64_t r = r0 + ro; r < r1; r += R) {
-        const double* xr = X + r * ld + s * K;
-        const double* yr = Y + r * ld + s * K;
+        const size_t base = (size_t)r * ld + (size_t)s * K;
         double v = 0.0;
-        for (int a = 0; a < K; ++a) v += (yr[a] - th * xr[a]) * __ldg(z + a * K + i);
+        for (int a = 0; a < K; ++a) {
+            const double y = Y1[base + a];
+            v += (X1 ? y - th * X1[base + a] : y) * __ldg(z1 + a * K + i);
+        }
+        if (Y2)
+            for (int a = 0; a < K; ++a) {
+                const double y = Y2[base + a];
+                v += (X2 ? y - th * X2[base + a] : y) * __ldg(z2 + a * K + i);
+            }
+        if (out) out[(size_t)r * ld + t] = v;
         acc += v * v;
     }
+    if (!part) return;
     s_red2[threadIdx.x] = acc;
     __syncthreads();
     if (ro == 0) {
@@ -1090,25 +1107,28 @@ __global__ void k_sum_cols(int nchunks, int ncols, const double* __restrict__ pa
 // host helpers
 // ---------------------------------------------------------------------------
 
-int sm_count() {
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess) return 132;
-        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 132;
-    }
-    return n;
+// Device attributes, looked up once per device ordinal.  The sectors of a
+// multi-sector call query them from several host threads at once, so each
+// cached value is an atomic (0 = not looked up yet; a racing lookup stores the
+// same value).
+static int device_attr_cached(std::atomic<int>* cache, cudaDeviceAttr attr, int fallback) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return fallback;
+    if (dev < 0 || dev >= kMaxDevices) return fallback;
+    int v = cache[dev].load(std::memory_order_relaxed);
+    if (v > 0) return v;
+    if (cudaDeviceGetAttribute(&v, attr, dev) != cudaSuccess || v <= 0) return fallback;
+    cache[dev].store(v, std::memory_order_relaxed);
+    return v;
 }
 
+static std::atomic<int> g_sm_count[kMaxDevices];
+static std::atomic<int> g_smem_optin[kMaxDevices];
+
+int sm_count() { return device_attr_cached(g_sm_count, cudaDevAttrMultiProcessorCount, 132); }
+
 static int max_smem_optin() {
-    static int v = 0;
-    if (v == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || v <= 0)
-            v = 48 * 1024;
-    }
-    return v;
+    return device_attr_cached(g_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, 48 * 1024);
 }
 
 // BH_VERBOSE=1 in the environment prints one line per restart to stderr.
@@ -1145,6 +1165,39 @@ static bool separate_local_dot() {
     return v == 1;
 }
 
+// BH_RITZ_MARGIN=k: Ritz vectors refined in FP64 beyond the wanted ones
+// (rounded up to whole blocks; default 0); BH_RITZ_STAGE2=0/1: the
+// residual-augmented second Rayleigh-Ritz of the mixed-precision refinement
+// (default 0); BH_KEEP_FRACTION=f: a thick restart keeps nev + f (ncv - nev)
+// Ritz vectors (default 0.5)
+static int ritz_margin() {
+    static int v = -1;
+    if (v < 0) {
+        const char* e = std::getenv("BH_RITZ_MARGIN");
+        v = (e && *e) ? std::max(0, std::atoi(e)) : 0;
+    }
+    return v;
+}
+
+static bool ritz_stage2() {
+    static int v = -1;
+    if (v < 0) {
+        const char* e = std::getenv("BH_RITZ_STAGE2");
+        v = (e && *e && *e != '0') ? 1 : 0;
+    }
+    return v == 1;
+}
+
+static double keep_fraction() {
+    static double v = -1.0;
+    if (v < 0.0) {
+        const char* e = std::getenv("BH_KEEP_FRACTION");
+        const double f = (e && *e) ? std::atof(e) : 0.5;
+        v = (f > 0.0 && f < 1.0) ? f : 0.5;
+    }
+    return v;
+}
+
 static bool debug_ortho() {
     static int v = -1;
     if (v < 0) {
@@ -1176,7 +1229,7 @@ static void parallel_for(int n, F&& f) {
     for (auto& t : th) t.join();
 }
 
-// geometry of the row-chunked reductions (k_dot, k_resid): at most 2 chunks per SM
+// geometry of the row-chunked reductions (k_dot, k_ritz_mix): at most 2 chunks per SM
 struct Geo {
     int ncols = 0, R = 1, NT = 0;
     int64_t rows_per_chunk = 0;
@@ -1477,6 +1530,54 @@ static bool cholesky_lower(int n, std::vector<double>& a) {  // a = L L^T, L in 
     return true;
 }
 
+// Generalised symmetric eigenproblem A z = theta G z of order n (column-major,
+// both symmetrised here), G positive definite: Cholesky G = L L^T, then the
+// standard problem L^{-1} A L^{-T}.  w receives the `want` lowest eigenvalues
+// (ascending), zz their vectors (column i at zz[i n ..]).  False if G is not
+// numerically positive definite or the eigensolve fails.
+static bool rayleigh_ritz(int n, std::vector<double> G, std::vector<double> A, int want,
+                          std::vector<double>& w, std::vector<double>& zz) {
+    for (int a = 0; a < n; ++a)
+        for (int b = a + 1; b < n; ++b) {
+            const double g = 0.5 * (G[(size_t)b * n + a] + G[(size_t)a * n + b]);
+            const double h = 0.5 * (A[(size_t)b * n + a] + A[(size_t)a * n + b]);
+            G[(size_t)b * n + a] = G[(size_t)a * n + b] = g;
+            A[(size_t)b * n + a] = A[(size_t)a * n + b] = h;
+        }
+    if (!cholesky_lower(n, G)) return false;
+    auto Lv = [&](int i, int j) { return G[(size_t)j * n + i]; };
+    std::vector<double> B(A);  // L B = A, column by column
+    for (int c = 0; c < n; ++c)
+        for (int i = 0; i < n; ++i) {
+            double v = B[(size_t)c * n + i];
+            for (int k = 0; k < i; ++k) v -= Lv(i, k) * B[(size_t)c * n + k];
+            B[(size_t)c * n + i] = v / Lv(i, i);
+        }
+    std::vector<double> M((size_t)n * n);  // M L^T = B, row by row
+    for (int r = 0; r < n; ++r)
+        for (int j = 0; j < n; ++j) {
+            double v = B[(size_t)j * n + r];
+            for (int k = 0; k < j; ++k) v -= M[(size_t)k * n + r] * Lv(j, k);
+            M[(size_t)j * n + r] = v / Lv(j, j);
+        }
+    for (int a = 0; a < n; ++a)
+        for (int b = a + 1; b < n; ++b) {
+            const double v = 0.5 * (M[(size_t)b * n + a] + M[(size_t)a * n + b]);
+            M[(size_t)b * n + a] = M[(size_t)a * n + b] = v;
+        }
+    std::vector<double> ev(n);
+    if (!symeig(n, M.data(), ev.data())) return false;
+    w.assign(ev.begin(), ev.begin() + want);
+    zz.assign((size_t)want * n, 0.0);
+    for (int i = 0; i < want; ++i)  // z = L^{-T} u
+        for (int a = n - 1; a >= 0; --a) {
+            double v = M[(size_t)i * n + a];
+            for (int k = a + 1; k < n; ++k) v -= Lv(k, a) * zz[(size_t)i * n + k];
+            zz[(size_t)i * n + a] = v / Lv(a, a);
+        }
+    return true;
+}
+
 // ---------------------------------------------------------------------------
 // the Lanczos phase (precision T for vectors)
 // ---------------------------------------------------------------------------
@@ -1517,6 +1618,8 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
     res.nconv.assign(S0, 0);
     res.conv_at.assign(S0, -1);
     res.scale.assign(S0, 1.0);
+    res.status.assign(S0, BH_OK);
+    res.live.assign(S0, kmax);
 
     std::vector<int> act(S0);  // original index of each active solve
     std::iota(act.begin(), act.end(), 0);
@@ -1791,12 +1894,20 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
         std::vector<int> fin, cont;  // active positions
         int minconv = rq.nev, ndead = 0;
         for (int a = 0; a < S; ++a) {
-            if (kuse[a] < rq.nev)
-                throw Error(BH_ERR_BREAKDOWN, "Krylov space exhausted before nev eigenvalues (dimension too small or invariant start block)");
             const int o = act[a];
             res.nconv[o] = nconv[a];
             res.scale[o] = hscale[a];
+            res.live[o] = kuse[a];
             ndead += kmax - kuse[a];
+            if (kuse[a] < rq.nev) {
+                // Krylov space exhausted before nev directions (an invariant
+                // start block, or a sector smaller than the request): retire
+                // the solve with the Ritz pairs it holds
+                res.status[o] = BH_ERR_BREAKDOWN;
+                fin.push_back(a);
+                minconv = std::min(minconv, nconv[a]);
+                continue;
+            }
             const bool conv_a = nconv[a] >= rq.nev;
             if (conv_a && res.conv_at[o] < 0) res.conv_at[o] = restarts;
             if (conv_a || last) fin.push_back(a);
@@ -1844,7 +1955,7 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
         if (cont.empty()) break;
 
         // thick restart of the continuing solves, compacted to the front
-        int nkeep = rq.nev + std::max(p, (kmax - rq.nev) / 2);
+        int nkeep = rq.nev + std::max(p, (int)(keep_fraction() * (kmax - rq.nev)));
         nkeep = (nkeep + p - 1) / p * p;
         nkeep = std::min(nkeep, kmax - 2 * p);
         if (nkeep < p) nkeep = p;
@@ -1951,8 +2062,12 @@ SolveResult block_lanczos(const OpView<double>& op64, const OpView<float>& op32,
     BH_REQUIRE(rq.kmax % p == 0 && (rq.kmax >= rq.nev + p || (rq.kmax == D && rq.kmax >= rq.nev)),
                "ncv must be a multiple of the block size and >= nev + block (or the whole space)");
     BH_REQUIRE((int64_t)rq.kmax <= D, "ncv exceeds the dimension");
-    const int K = (rq.nev + p - 1) / p * p;  // Ritz vectors refined in FP64
-    BH_REQUIRE(K <= 32 && K <= rq.kmax, "too many wanted eigenvalues for this block size");
+    const int K0 = (rq.nev + p - 1) / p * p;  // Ritz vectors needed
+    BH_REQUIRE(K0 <= 32 && K0 <= rq.kmax, "too many wanted eigenvalues for this block size");
+    // Ritz vectors refined in FP64: the wanted ones plus a margin (whole
+    // blocks), so that the Rayleigh-Ritz error of the highest wanted values is
+    // set by their gap to the first level outside the refined space
+    const int K = std::max(K0, std::min({32, rq.kmax, (rq.nev + ritz_margin() + p - 1) / p * p}));
 
     // per-solve parameters (J, U, shift) and start scale
     std::vector<double> prm((size_t)3 * S);
@@ -1980,7 +2095,11 @@ SolveResult block_lanczos(const OpView<double>& op64, const OpView<float>& op32,
         lanczos_phase<double>(op64, rq, prm, st, res, K, X64, theta0);
     }
 
-    // ---- FP64 Rayleigh-Ritz refinement on the K Ritz vectors per solve ----
+    // ---- FP64 refinement of the K Ritz vectors per solve ----
+    // Stage 1: Rayleigh-Ritz on X (FP64 product, FP64 Gram matrices).
+    // Stage 2 (mixed precision, BH_RITZ_STAGE2=1): Rayleigh-Ritz on [X, R]
+    // with the stage-1 residual vectors R = H X z_i - theta_i X z_i (one
+    // step of a block Davidson iteration without preconditioner).
     const int nc2 = S * K;
     Launcher<double> L{op64, st, &res.launches};
     DevBuf<double> Y64((size_t)D * nc2);
@@ -1989,97 +2108,165 @@ SolveResult block_lanczos(const OpView<double>& op64, const OpView<float>& op32,
     // Gram matrices per solve, in groups of at most 512 columns
     const int sgrp = std::max(1, std::min(S, 512 / K));
     const Geo gmax = make_geo(D, sgrp * K);
-    DevBuf<double> part((size_t)gmax.nchunks * K * sgrp * K), Gd((size_t)K * nc2), Ad((size_t)K * nc2);
-    for (int s0 = 0; s0 < S; s0 += sgrp) {
-        const int ns = std::min(sgrp, S - s0);
-        const Geo gg = make_geo(D, ns * K);
-        const int64_t off = (int64_t)s0 * K;
-        L.dot(gg, nc2, K, 1, 0, X64.p + off, X64.p + off, K, part.p);
-        L.dot_finalize(gg, K, nc2, K, K, part.p, Gd.p + off, nullptr, nullptr, 0, 0);
-        L.dot(gg, nc2, K, 1, 0, X64.p + off, Y64.p + off, K, part.p);
-        L.dot_finalize(gg, K, nc2, K, K, part.p, Ad.p + off, nullptr, nullptr, 0, 0);
-    }
-    std::vector<double> hG((size_t)K * nc2), hA((size_t)K * nc2);
-    BH_CUDA(cudaMemcpyAsync(hG.data(), Gd.p, hG.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-    BH_CUDA(cudaMemcpyAsync(hA.data(), Ad.p, hA.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    DevBuf<double> part((size_t)gmax.nchunks * K * sgrp * K), rpart((size_t)gmax.nchunks * sgrp * K);
+    // C[a * nc2 + s K + b] = sum_r A[r][s K + a] B[r][s K + b] for every solve
+    auto gram = [&](const double* A, const double* B, DevBuf<double>& C) {
+        if (C.n < (size_t)K * nc2) C.alloc((size_t)K * nc2);
+        for (int s0 = 0; s0 < S; s0 += sgrp) {
+            const int ns = std::min(sgrp, S - s0);
+            const Geo gg = make_geo(D, ns * K);
+            const int64_t off = (int64_t)s0 * K;
+            L.dot(gg, nc2, K, 1, 0, A + off, B + off, K, part.p);
+            L.dot_finalize(gg, K, nc2, K, K, part.p, C.p + off, nullptr, nullptr, 0, 0);
+        }
+    };
+    auto to_host = [&](const DevBuf<double>& C) {
+        std::vector<double> h((size_t)K * nc2);
+        BH_CUDA(cudaMemcpyAsync(h.data(), C.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+        return h;
+    };
+    // out (optional) and/or squared-norm partials of the columns
+    //   sum_a (Y1 - theta X1)[:, a] Z1[a][i] + sum_a (Y2 - theta X2)[:, a] Z2[a][i]
+    auto mix = [&](const double* Y1, const double* X1, const double* Z1, const double* Y2,
+                   const double* X2, const double* Z2, const double* theta, double* out,
+                   double* norms) {
+        for (int s0 = 0; s0 < S; s0 += sgrp) {
+            const int ns = std::min(sgrp, S - s0);
+            const Geo gg = make_geo(D, ns * K);
+            const int64_t off = (int64_t)s0 * K;
+            const int64_t zoff = off * K;
+            k_ritz_mix<<<gg.nchunks, gg.NT, norms ? gg.NT * sizeof(double) : 0, st>>>(
+                D, ns * K, nc2, K, Y1 + off, X1 ? X1 + off : nullptr, Z1 + zoff, Y2 ? Y2 + off : nullptr,
+                X2 ? X2 + off : nullptr, Z2 ? Z2 + zoff : nullptr, theta ? theta + off : nullptr,
+                out ? out + off : nullptr, gg.rows_per_chunk, norms ? rpart.p : nullptr);
+            BH_CUDA(cudaGetLastError());
+            ++res.launches;
+            if (norms) {
+                k_sum_cols<<<(ns * K + 255) / 256, 256, 0, st>>>(gg.nchunks, ns * K, rpart.p, norms + off);
+                BH_CUDA(cudaGetLastError());
+                ++res.launches;
+            }
+        }
+    };
+    DevBuf<double> Gd, Ad;
+    gram(X64.p, X64.p, Gd);
+    gram(X64.p, Y64.p, Ad);
+    const std::vector<double> hG = to_host(Gd), hA = to_host(Ad);
     BH_CUDA(cudaStreamSynchronize(st));
-    std::vector<double> th((size_t)nc2), Z((size_t)S * K * K);
-    bool fail = false;
+    const double nan = std::numeric_limits<double>::quiet_NaN();
+    std::vector<double> th((size_t)nc2, nan), Z((size_t)S * K * K, 0.0);
+    std::vector<int> kref(S, K);  // Ritz vectors refined per solve
     parallel_for(S, [&](int s) {
-        // G_s[a][b] is at hG[a * nc2 + s K + b]
-        std::vector<double> Gm((size_t)K * K), Am((size_t)K * K);
-        for (int a = 0; a < K; ++a)
-            for (int b = 0; b < K; ++b) {
-                Gm[(size_t)b * K + a] = 0.5 * (hG[(size_t)a * nc2 + s * K + b] + hG[(size_t)b * nc2 + s * K + a]);
-                Am[(size_t)b * K + a] = 0.5 * (hA[(size_t)a * nc2 + s * K + b] + hA[(size_t)b * nc2 + s * K + a]);
+        // a solve whose Krylov space broke down holds only res.live[s] Ritz
+        // vectors (the rest are zero): the refinement uses those
+        const int k = std::min(K, std::max(0, res.live[s]));
+        kref[s] = k;
+        if (k == 0) return;
+        std::vector<double> Gm((size_t)k * k), Am((size_t)k * k), w, zz;
+        for (int a = 0; a < k; ++a)
+            for (int b = 0; b < k; ++b) {
+                Gm[(size_t)b * k + a] = hG[(size_t)a * nc2 + s * K + b];
+                Am[(size_t)b * k + a] = hA[(size_t)a * nc2 + s * K + b];
             }
-        if (!cholesky_lower(K, Gm)) {
-            fail = true;
+        if (!rayleigh_ritz(k, Gm, Am, k, w, zz)) {
+            kref[s] = 0;
+            if (res.status[s] == BH_OK) res.status[s] = BH_ERR_NOCONV;
             return;
         }
-        // M = L^{-1} A L^{-T}
-        auto Lv = [&](int i, int j) { return Gm[(size_t)j * K + i]; };
-        std::vector<double> B(Am);  // solve L B = A (column by column)
-        for (int c = 0; c < K; ++c)
-            for (int i = 0; i < K; ++i) {
-                double v = B[(size_t)c * K + i];
-                for (int k = 0; k < i; ++k) v -= Lv(i, k) * B[(size_t)c * K + k];
-                B[(size_t)c * K + i] = v / Lv(i, i);
-            }
-        std::vector<double> M((size_t)K * K);  // M = B L^{-T}: solve M L^T = B  -> rows
-        for (int r = 0; r < K; ++r)
-            for (int j = 0; j < K; ++j) {
-                double v = B[(size_t)j * K + r];
-                for (int k = 0; k < j; ++k) v -= M[(size_t)k * K + r] * Lv(j, k);
-                M[(size_t)j * K + r] = v / Lv(j, j);
-            }
-        for (int a = 0; a < K; ++a)
-            for (int b = a + 1; b < K; ++b) {
-                const double v = 0.5 * (M[(size_t)b * K + a] + M[(size_t)a * K + b]);
-                M[(size_t)b * K + a] = M[(size_t)a * K + b] = v;
-            }
-        std::vector<double> w(K);
-        if (!symeig(K, M.data(), w.data())) {
-            fail = true;
-            return;
-        }
-        // z = L^{-T} u
-        for (int i = 0; i < K; ++i) {
+        // Z_s is K x K (entry [a][i] at (s K + a) K + i); rows and columns beyond k stay zero
+        for (int i = 0; i < k; ++i) {
             th[(size_t)s * K + i] = w[i];
-            for (int a = K - 1; a >= 0; --a) {
-                double v = M[(size_t)i * K + a];
-                for (int k = a + 1; k < K; ++k) v -= Lv(k, a) * Z[((size_t)s * K + k) * K + i];
-                Z[((size_t)s * K + a) * K + i] = v / Lv(a, a);
-            }
+            for (int a = 0; a < k; ++a) Z[((size_t)s * K + a) * K + i] = zz[(size_t)i * k + a];
         }
     });
-    if (fail) throw Error(BH_ERR_NOCONV, "final Rayleigh-Ritz failed (Ritz vectors not independent)");
-    DevBuf<double> d_th(nc2), d_Z(Z.size()), rpart((size_t)gmax.nchunks * sgrp * K), rn(nc2);
+    DevBuf<double> d_th(nc2), d_Z(Z.size()), rn(nc2);
     BH_CUDA(cudaMemcpyAsync(d_th.p, th.data(), nc2 * sizeof(double), cudaMemcpyHostToDevice, st));
     BH_CUDA(cudaMemcpyAsync(d_Z.p, Z.data(), Z.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-    for (int s0 = 0; s0 < S; s0 += sgrp) {
-        const int ns = std::min(sgrp, S - s0);
-        const Geo gg = make_geo(D, ns * K);
-        const int64_t off = (int64_t)s0 * K;
-        k_resid<<<gg.nchunks, gg.NT, gg.NT * sizeof(double), st>>>(
-            D, ns * K, nc2, K, X64.p + off, Y64.p + off, d_th.p + off, d_Z.p + off * K,
-            gg.rows_per_chunk, rpart.p);
-        BH_CUDA(cudaGetLastError());
-        k_sum_cols<<<(ns * K + 255) / 256, 256, 0, st>>>(gg.nchunks, ns * K, rpart.p, rn.p + off);
-        BH_CUDA(cudaGetLastError());
-        res.launches += 2;
+
+    std::vector<double> Zr((size_t)S * K * K, 0.0);  // stage-2 coefficients on R (zero: not used)
+    DevBuf<double> Rb, HRb;
+    const bool stage2 = rq.precision == BH_PREC_MIXED && ritz_stage2();
+    if (stage2) {
+        Rb.alloc((size_t)D * nc2);
+        HRb.alloc((size_t)D * nc2);
+        mix(Y64.p, X64.p, d_Z.p, nullptr, nullptr, nullptr, d_th.p, Rb.p, nullptr);
+        L.spmm(nc2, K, d_prm.p, Rb.p, HRb.p);
+        res.matvecs += K;
+        DevBuf<double> Gxr, Grr, Axh, Arh;
+        gram(X64.p, Rb.p, Gxr);
+        gram(Rb.p, Rb.p, Grr);
+        gram(X64.p, HRb.p, Axh);
+        gram(Rb.p, HRb.p, Arh);
+        const std::vector<double> hGxr = to_host(Gxr), hGrr = to_host(Grr), hAxh = to_host(Axh),
+                                  hArh = to_host(Arh);
+        BH_CUDA(cudaStreamSynchronize(st));
+        parallel_for(S, [&](int s) {
+            if (res.status[s] != BH_OK || kref[s] < K) return;
+            // residual directions above FP64 noise of the spectrum's scale,
+            // each scaled to unit norm
+            const double noise = 1e-13 * std::max(1.0, res.scale[s]);
+            std::vector<int> keep;
+            std::vector<double> sig;
+            for (int b = 0; b < K; ++b) {
+                const double g = hGrr[(size_t)b * nc2 + s * K + b];
+                if (g > noise * noise) {
+                    keep.push_back(b);
+                    sig.push_back(1.0 / std::sqrt(g));
+                }
+            }
+            const int kr = (int)keep.size();
+            if (kr == 0) return;
+            const int n2 = K + kr;
+            auto G = [&](const std::vector<double>& h, int a, int b) { return h[(size_t)a * nc2 + s * K + b]; };
+            std::vector<double> G2((size_t)n2 * n2), A2((size_t)n2 * n2), w, zz;
+            for (int a = 0; a < n2; ++a)
+                for (int b = 0; b < n2; ++b) {
+                    double g, h;
+                    if (a < K && b < K) {
+                        g = G(hG, a, b);
+                        h = G(hA, a, b);
+                    } else if (a < K) {  // X_a^T r_b
+                        const int rb = keep[b - K];
+                        g = G(hGxr, a, rb) * sig[b - K];
+                        h = G(hAxh, a, rb) * sig[b - K];
+                    } else if (b < K) {  // r_a^T X_b
+                        const int ra = keep[a - K];
+                        g = G(hGxr, b, ra) * sig[a - K];
+                        h = G(hAxh, b, ra) * sig[a - K];
+                    } else {
+                        const int ra = keep[a - K], rb = keep[b - K];
+                        g = G(hGrr, ra, rb) * sig[a - K] * sig[b - K];
+                        h = G(hArh, ra, rb) * sig[a - K] * sig[b - K];
+                    }
+                    G2[(size_t)b * n2 + a] = g;
+                    A2[(size_t)b * n2 + a] = h;
+                }
+            if (!rayleigh_ritz(n2, G2, A2, K, w, zz)) return;  // keep the stage-1 pairs
+            for (int i = 0; i < K; ++i) {
+                th[(size_t)s * K + i] = w[i];
+                for (int a = 0; a < K; ++a) Z[((size_t)s * K + a) * K + i] = zz[(size_t)i * n2 + a];
+                for (int q = 0; q < kr; ++q)
+                    Zr[((size_t)s * K + keep[q]) * K + i] = zz[(size_t)i * n2 + K + q] * sig[q];
+            }
+        });
+        BH_CUDA(cudaMemcpyAsync(d_th.p, th.data(), nc2 * sizeof(double), cudaMemcpyHostToDevice, st));
+        BH_CUDA(cudaMemcpyAsync(d_Z.p, Z.data(), Z.size() * sizeof(double), cudaMemcpyHostToDevice, st));
     }
+    DevBuf<double> d_Zr;
+    if (stage2) {
+        d_Zr.alloc(Zr.size());
+        BH_CUDA(cudaMemcpyAsync(d_Zr.p, Zr.data(), Zr.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    }
+    // true residual norms ||H x_i - theta_i x_i||^2 of the returned pairs
+    mix(Y64.p, X64.p, d_Z.p, stage2 ? HRb.p : nullptr, stage2 ? Rb.p : nullptr, stage2 ? d_Zr.p : nullptr,
+        d_th.p, nullptr, rn.p);
     std::vector<double> hrn(nc2);
     BH_CUDA(cudaMemcpyAsync(hrn.data(), rn.p, nc2 * sizeof(double), cudaMemcpyDeviceToHost, st));
     DevBuf<double> Xf;
-    DevBuf<int> d_id;
     if (rq.want_vectors) {
-        std::vector<int> id(S);
-        std::iota(id.begin(), id.end(), 0);
-        d_id.alloc(S);
-        BH_CUDA(cudaMemcpyAsync(d_id.p, id.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
         Xf.alloc((size_t)D * nc2);
-        L.rotate(S, nc2, K, K, K, 0, X64.p, d_Z.p, d_id.p, d_id.p, Xf.p, 0, nc2, 1);
+        mix(X64.p, nullptr, d_Z.p, stage2 ? Rb.p : nullptr, nullptr, stage2 ? d_Zr.p : nullptr, nullptr,
+            Xf.p, nullptr);
     }
     BH_CUDA(cudaStreamSynchronize(st));
 
@@ -2087,13 +2274,16 @@ SolveResult block_lanczos(const OpView<double>& op64, const OpView<float>& op32,
     const double eps23 = std::pow(2.220446049250313e-16, 2.0 / 3.0);
     res.evals.assign((size_t)S * nev, 0.0);
     res.resid.assign((size_t)S * nev, 0.0);
-    for (int s = 0; s < S; ++s)
+    for (int s = 0; s < S; ++s) {
         for (int i = 0; i < nev; ++i) {
             const double e = th[(size_t)s * K + i];
             res.evals[(size_t)s * nev + i] = e;
             const double fl = std::max(eps23, 1e-3 * res.scale[s]);
-            res.resid[(size_t)s * nev + i] = std::sqrt(std::max(0.0, hrn[(size_t)s * K + i])) / std::max(std::fabs(e), fl);
+            res.resid[(size_t)s * nev + i] =
+                i < kref[s] ? std::sqrt(std::max(0.0, hrn[(size_t)s * K + i])) / std::max(std::fabs(e), fl) : nan;
         }
+        res.nconv[s] = std::min(res.nconv[s], kref[s]);
+    }
     profile_flush();
     if (rq.want_vectors) {
         std::vector<double> hx((size_t)D * nc2);

@@ -100,6 +100,11 @@ struct SolveResult {
     std::vector<int> conv_at;    // S: restart count at which the solve converged (-1: never)
     std::vector<double> scale;   // S: spectral radius estimate (largest |Ritz value|)
     std::vector<double> vecs;    // S x nev x D (lexicographic/operator order), if requested
+    std::vector<int> status;     // S: BH_OK, or BH_ERR_BREAKDOWN where the solve's Krylov
+                                 // space held fewer than nev directions (an invariant start
+                                 // block), or BH_ERR_NOCONV where its Ritz vectors were not
+                                 // independent in the final Rayleigh-Ritz
+    std::vector<int> live;       // S: Krylov directions the solve held at its last restart
     int restarts = 0;
     int64_t matvecs = 0;
     int64_t launches = 0;        // kernels launched by the solve

@@ -19,7 +19,10 @@
 // contents of the last call; every word a call reads is written by the same
 // call first (nothing needs to start at zero).  Calls that overlap on the GPU
 // (different streams, or several host threads) race on the array and must be
-// serialised by the caller.
+// serialised by the caller.  The cached address belongs to the device's
+// current context: after a cudaDeviceReset the process must not call this
+// entry point again on that device.  In the lexicographic order the product
+// reads x while it writes y, so x and y must not overlap (checked).
 #include <mutex>
 
 #include "bh_internal.h"
@@ -76,6 +79,13 @@ extern "C" int bh_hamiltonian_apply_noalloc(const bh_hamiltonian* h, int order, 
                                             " doubles exceeds the fixed scratch of " +
                                             std::to_string(bh::kApplyScratchDoubles - bh::kApplyParamWords) +
                                             " doubles (32 MiB); use bh_hamiltonian_apply or fewer vectors");
+        if (order == BH_ORDER_LEX) {
+            // the product gathers rows of x while it writes y
+            const uintptr_t n = (uintptr_t)(D * (int64_t)nvec) * sizeof(double);
+            const uintptr_t xa = reinterpret_cast<uintptr_t>(x), ya = reinterpret_cast<uintptr_t>(y);
+            BH_REQUIRE(xa + n <= ya || ya + n <= xa,
+                       "bh_hamiltonian_apply_noalloc: x and y overlap (not allowed in the lexicographic order)");
+        }
         int dev = 0;
         BH_CUDA(cudaGetDevice(&dev));
         BH_REQUIRE(dev == h->device, "the current device is not the Hamiltonian's device");

@@ -141,9 +141,12 @@ int bh_hamiltonian_apply(const bh_hamiltonian* h, int order, double J, double U,
  * (4 Mi doubles), shared by all calls and kept by every GPU that loads the
  * library until exit, so 2 * D * nvec must not exceed 4 Mi - 32 doubles in
  * the reference order (BH_ERR_ARG otherwise; the lexicographic order needs no
- * vector scratch).  The first call on each device looks up that array's
- * device address and should come before any stream capture.  Calls that
- * overlap on the GPU race on the shared array: serialise them. */
+ * vector scratch, but there x and y must not overlap: BH_ERR_ARG).  The first
+ * call on each device looks up that array's device address and should come
+ * before any stream capture; the address is kept for the device's context, so
+ * after a cudaDeviceReset the process must not call this entry point again on
+ * that device.  Calls that overlap on the GPU race on the shared array:
+ * serialise them. */
 int bh_hamiltonian_apply_noalloc(const bh_hamiltonian* h, int order, double J, double U,
                                  double mu, int nvec, const double* x, double* y, void* stream);
 
@@ -177,7 +180,11 @@ void bh_solver_opts_default(bh_solver_opts* o);
 /* Replaces Op::IRLM_eigen (operator.cpp:22-33) for one (J, U, mu) point of a
  * built Hamiltonian: the nev lowest eigenvalues, ascending, in evals[nev];
  * per-pair relative residuals in resid[nev] (may be NULL); Ritz vectors in
- * evecs[nev*D] (row i = vector i, in opts->order; may be NULL). */
+ * evecs[nev*D] (row i = vector i, in opts->order; may be NULL).  Returns
+ * BH_ERR_NOCONV ("Eigenvalue computation failed.") when fewer than nev pairs
+ * converged and BH_ERR_BREAKDOWN when the Krylov space was exhausted first.
+ * Every entry point rejects non-finite J, U, mu (and tol, matrix values)
+ * with BH_ERR_ARG before any device work. */
 int bh_eigsh(const bh_hamiltonian* h, double J, double U, double mu, const bh_solver_opts* o,
              double* evals, double* resid, double* evecs, bh_solve_info* info);
 
@@ -196,6 +203,21 @@ int bh_eigsh_csr(int64_t dim, const int64_t* row_ptr, const int32_t* col, const 
 int bh_eigsh_batch(const bh_hamiltonian* h, int nsolve, const double* J, const double* U,
                    const double* mu, const bh_solver_opts* o, double* evals, double* resid,
                    int* nconv, bh_solve_info* info);
+/* bh_eigsh_batch with a status per point (the reference's grid loop calls
+ * Op::IRLM_eigen per point, which throws std::runtime_error("Eigenvalue
+ * computation failed.") on non-convergence, operator.cpp:27-29, and Spectra
+ * throws on an exhausted Krylov space, GenEigsBase.h:335-339):
+ * status[nsolve] receives BH_OK, BH_ERR_NOCONV (fewer than nev pairs
+ * converged within max_restarts, or Ritz vectors not independent in the final
+ * FP64 refinement) or BH_ERR_BREAKDOWN (the point's Krylov space held fewer
+ * than nev directions: an invariant start block, e.g. H a multiple of the
+ * identity; its evals hold the values it found, NaN beyond them).  The call
+ * itself returns BH_OK when it ran; one failing point does not stop the
+ * others.  bh_eigsh_batch is this call without status (nconv[s] < nev marks a
+ * failed point there). */
+int bh_eigsh_batch_status(const bh_hamiltonian* h, int nsolve, const double* J, const double* U,
+                          const double* mu, const bh_solver_opts* o, double* evals, double* resid,
+                          int* nconv, int* status, bh_solve_info* info);
 /* bh_eigsh_batch with the eigenvectors: evecs[(s*nev + i)*D + r] (host,
  * D*nev doubles per solve, rows in o->order), the i-th lowest eigenvector of
  * solve s (FP64 Rayleigh-Ritz vectors of either precision). */

@@ -98,3 +98,18 @@ def test_spdm_matches_oracle(pkg, orc):
     cf = orc.condensate_fraction(rho_o)
     assert 0.0 < cf <= 1.0
     assert abs(pkg.Analysis.coherence(rho) - orc.coherence(rho_o)) < 1e-10
+
+
+def test_mixed_matches_fp64_pure_relative_on_the_bench_grid(pkg):
+    # every eigenvalue of the benchmark grid (m = 10, n = 8..12, 64 J in
+    # (0, 0.3], lowest 10) from the mixed-precision batch within 1e-8 of the
+    # FP64 batch relative to its own magnitude, with no absolute floor (the
+    # levels near zero are the hardest case)
+    Js = 0.3 * (np.arange(64) + 1) / 64
+    lists = chain_lists(10)
+    hams = [pkg.Hamiltonian(pkg.Basis(10, n), lists) for n in (8, 9, 10, 11, 12)]
+    ev_m, _, nc_m, _ = pkg.eigsh_sectors(hams, Js, 1.0, 0.0, nev=10, precision=pkg.PREC_MIXED)
+    ev_d, _, nc_d, _ = pkg.eigsh_sectors(hams, Js, 1.0, 0.0, nev=10, precision=pkg.PREC_FP64)
+    assert nc_m.min() == 10 and nc_d.min() == 10
+    rel = np.abs(ev_m - ev_d) / np.abs(ev_d)
+    assert rel.max() < 1e-8, (rel.max(), np.unravel_index(rel.argmax(), rel.shape))

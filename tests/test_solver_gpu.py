@@ -115,3 +115,23 @@ def test_nonconvergence_is_reported(pkg):
     h = pkg.Hamiltonian(pkg.Basis(8, 8), chain_lists(8))
     with pytest.raises(pkg.BHError, match="Eigenvalue computation failed"):
         h.eigsh(0.1, 1.0, 0.5, nev=10, max_restarts=1, ncv=22)
+
+
+def test_exact_eigen_matches_reference_dense_spectra(pkg, orc, golden):
+    # Op::exact_eigen (operator.cpp:92-101): every eigenvalue of the dense
+    # Hamiltonian, ascending, against the reference's own Eigen
+    # SelfAdjointEigenSolver run on the same matrices
+    for key, want in golden["exact_eigen"].items():
+        m, n, J, U, mu = key.split(",")
+        m, n, J, U, mu = int(m), int(n), float(J), float(U), float(mu)
+        _, _, _, rp, ci, tv, vd = oracle_H(orc, m, n, chain_lists(m))
+        H = orc.full_csr(rp, ci, tv, vd, n, J, U, mu)
+        w, z = pkg.Op.exact_eigen(H)
+        want = np.array(want)
+        assert w.shape == want.shape
+        scale = max(1.0, np.abs(want).max())
+        np.testing.assert_allclose(w, want, rtol=1e-12, atol=1e-12 * scale)
+        # the eigenvectors: orthonormal columns with H z = z diag(w)
+        Hd = H.toarray()
+        np.testing.assert_allclose(z.T @ z, np.eye(len(w)), atol=1e-12)
+        np.testing.assert_allclose(Hd @ z, z * w, atol=1e-11 * scale)

@@ -57,3 +57,20 @@ def test_noalloc_apply_rejects_sizes_beyond_the_fixed_scratch(pkg):
     rc, _ = _call(pkg, h, pkg.ORDER_REFERENCE, 0.1, 1.0, 0.0, x)
     assert rc == pkg.BH_ERR_ARG
     assert b"exceeds the fixed scratch" in pkg.load().bh_last_error()
+
+
+def test_noalloc_apply_rejects_overlapping_buffers_in_lex_order(pkg):
+    # the lexicographic product reads rows of x while it writes y: one buffer
+    # for both is refused before any launch
+    import torch
+
+    m, n = 6, 4
+    h = pkg.Hamiltonian(pkg.Basis(m, n), chain_lists(m))
+    xd = torch.zeros((h.D, 2), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    lib = pkg.load()
+    rc = lib.bh_hamiltonian_apply_noalloc(h._h, pkg.ORDER_LEX, 0.1, 1.0, 0.0, 2,
+                                          C.c_void_p(xd.data_ptr()), C.c_void_p(xd.data_ptr()),
+                                          C.c_void_p(stream.cuda_stream))
+    assert rc == pkg.BH_ERR_ARG
+    assert b"overlap" in lib.bh_last_error()
