@@ -36,54 +36,10 @@
 #include <utility>
 #include <vector>
 
+#include "bh_cxx.hpp"
 #include "bh_gb300.h"
 
 namespace bhgb {
-
-inline void check(int rc) {
-    if (rc == BH_OK) return;
-    const std::string msg = bh_last_error();
-    if (rc == BH_ERR_NOCONV) throw std::runtime_error("Eigenvalue computation failed.");
-    if (rc == BH_ERR_ARG) throw std::invalid_argument(msg);
-    throw std::runtime_error(msg);
-}
-
-inline void flatten(const std::vector<std::vector<int>>& nb, std::vector<int32_t>& off,
-                    std::vector<int32_t>& flat) {
-    off.assign(nb.size() + 1, 0);
-    flat.clear();
-    for (size_t i = 0; i < nb.size(); ++i) {
-        for (int j : nb[i]) flat.push_back(j);
-        off[i + 1] = (int32_t)flat.size();
-    }
-    if (flat.empty()) flat.push_back(0);
-}
-
-// owning wrappers of the C handles
-struct Basis {
-    bh_basis* p = nullptr;
-    Basis(int m, int n) { check(bh_basis_create(m, n, &p)); }
-    ~Basis() { bh_basis_destroy(p); }
-    Basis(const Basis&) = delete;
-    Basis& operator=(const Basis&) = delete;
-    int64_t dim() const {
-        int64_t d = 0;
-        check(bh_basis_info(p, nullptr, nullptr, &d));
-        return d;
-    }
-};
-
-struct Hamiltonian {
-    bh_hamiltonian* p = nullptr;
-    Hamiltonian(const Basis& b, const std::vector<std::vector<int>>& nb) {
-        std::vector<int32_t> off, flat;
-        flatten(nb, off, flat);
-        check(bh_hamiltonian_create(b.p, off.data(), flat.data(), &p));
-    }
-    ~Hamiltonian() { bh_hamiltonian_destroy(p); }
-    Hamiltonian(const Hamiltonian&) = delete;
-    Hamiltonian& operator=(const Hamiltonian&) = delete;
-};
 
 // CSR (symmetric matrix) -> Eigen::SparseMatrix<double> (ColMajor): for a
 // symmetric matrix the row-compressed arrays are the column-compressed ones.
@@ -108,14 +64,8 @@ inline Eigen::SparseMatrix<double> term(const std::vector<std::vector<int>>& nb,
                                         bool keep_off) {
     Basis b(m, n);
     Hamiltonian h(b, nb);
-    const int64_t D = b.dim();
-    int64_t nnz = 0;
-    check(bh_hamiltonian_nnz(h.p, &nnz));
-    std::vector<int64_t> rp(D + 1);
-    std::vector<int32_t> ci(nnz + D);
-    std::vector<double> val(nnz + D);
-    check(bh_hamiltonian_csr(h.p, BH_ORDER_REFERENCE, J, U, mu, rp.data(), ci.data(), val.data()));
-    return from_csr(D, rp, ci, val, keep_diag, keep_off);
+    const Csr c = hamiltonian_csr(b, h, J, U, mu);
+    return from_csr(c.dim, c.rp, c.ci, c.val, keep_diag, keep_off);
 }
 
 // the reference's sort_basis (hamiltonian.cpp:109-123): argsort by tag, then
@@ -133,18 +83,15 @@ inline void sort_like_reference(Eigen::VectorXd& tags, Eigen::MatrixXd& basis) {
         }
 }
 
-inline void csr_of(Eigen::SparseMatrix<double>& O, std::vector<int64_t>& rp, std::vector<int32_t>& ci,
-                   std::vector<double>& val) {
+inline Csr csr_of(Eigen::SparseMatrix<double>& O) {
     O.makeCompressed();
-    const int64_t D = O.rows();
-    rp.resize(D + 1);
-    for (int64_t c = 0; c <= D; ++c) rp[c] = O.outerIndexPtr()[c];
-    ci.assign(O.innerIndexPtr(), O.innerIndexPtr() + O.nonZeros());
-    val.assign(O.valuePtr(), O.valuePtr() + O.nonZeros());
-    if (ci.empty()) {
-        ci.push_back(0);
-        val.push_back(0.0);
-    }
+    Csr c;
+    c.dim = O.rows();
+    c.rp.resize(c.dim + 1);
+    for (int64_t k = 0; k <= c.dim; ++k) c.rp[k] = O.outerIndexPtr()[k];
+    c.ci.assign(O.innerIndexPtr(), O.innerIndexPtr() + O.nonZeros());
+    c.val.assign(O.valuePtr(), O.valuePtr() + O.nonZeros());
+    return c;
 }
 
 }  // namespace bhgb
@@ -154,20 +101,6 @@ inline void csr_of(Eigen::SparseMatrix<double>& O, std::vector<int64_t>& rp, std
 // ---- Neighbours (neighbours.hpp:20-58) ----
 Neighbours::Neighbours(int m) : m(m), neighbours(m) {}
 Neighbours::~Neighbours() {}
-
-namespace bhgb {
-template <class F>
-std::vector<std::vector<int>> lattice(int m, bool closed, F fn) {
-    std::vector<int32_t> off(m + 1);
-    int count = 0;
-    check(fn(m, closed ? 1 : 0, off.data(), nullptr, 0, &count));
-    std::vector<int32_t> flat(count > 0 ? count : 1);
-    check(fn(m, closed ? 1 : 0, off.data(), flat.data(), (int)flat.size(), &count));
-    std::vector<std::vector<int>> out(m);
-    for (int i = 0; i < m; ++i) out[i].assign(flat.begin() + off[i], flat.begin() + off[i + 1]);
-    return out;
-}
-}  // namespace bhgb
 
 void Neighbours::chain_neighbours(bool closed) { neighbours = bhgb::lattice(m, closed, bh_neighbours_chain); }
 void Neighbours::square_neighbours(bool closed) { neighbours = bhgb::lattice(m, closed, bh_neighbours_square); }
@@ -281,42 +214,18 @@ void BH::h_MF(double psi, int p, double mu, double J, int q, Eigen::MatrixXd& h)
 }
 
 // ---- Op (operator.hpp:17-55) ----
-namespace bhgb {
-inline void eigsh(Eigen::SparseMatrix<double>& O, int nev, std::vector<double>& ev,
-                  std::vector<double>& vec) {
-    std::vector<int64_t> rp;
-    std::vector<int32_t> ci;
-    std::vector<double> val;
-    csr_of(O, rp, ci, val);
-    bh_solver_opts o;
-    bh_solver_opts_default(&o);
-    o.nev = nev;
-    o.want_vectors = 1;
-    o.order = BH_ORDER_LEX;  // the caller's own order (identity map)
-    ev.assign(nev, 0.0);
-    vec.assign((size_t)nev * O.rows(), 0.0);
-    bh_solve_info info;
-    check(bh_eigsh_csr(O.rows(), rp.data(), ci.data(), val.data(), &o, ev.data(), nullptr,
-                       vec.data(), &info));
-}
-}  // namespace bhgb
-
 // Lowest nb_eigen eigenpairs of the symmetric O, ordered like Spectra's
-// LargestMagn output (GenEigsBase.h:417, 466-483), as complex vectors.
+// LargestMagn output (GenEigsBase.h:417, 466-483), as complex vectors
+// (bhgb::irlm_eigen, bh_cxx.hpp).
 Eigen::VectorXcd Op::IRLM_eigen(Eigen::SparseMatrix<double> O, int nb_eigen, Eigen::MatrixXcd& eigenvectors) {
-    if (nb_eigen < 1 || nb_eigen > O.rows() - 2)
-        throw std::invalid_argument("nev must satisfy 1 <= nev <= n - 2, n is the size of matrix");
     std::vector<double> ev, vec;
-    bhgb::eigsh(O, nb_eigen, ev, vec);
-    std::vector<int> ord(nb_eigen);
-    for (int i = 0; i < nb_eigen; ++i) ord[i] = i;
-    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return std::fabs(ev[a]) > std::fabs(ev[b]); });
+    bhgb::irlm_eigen(bhgb::csr_of(O), nb_eigen, ev, vec);
     Eigen::VectorXcd vals(nb_eigen);
     eigenvectors.resize(O.rows(), nb_eigen);
     for (int k = 0; k < nb_eigen; ++k) {
-        vals[k] = std::complex<double>(ev[ord[k]], 0.0);
+        vals[k] = std::complex<double>(ev[k], 0.0);
         for (Eigen::Index r = 0; r < O.rows(); ++r)
-            eigenvectors(r, k) = std::complex<double>(vec[(size_t)ord[k] * O.rows() + r], 0.0);
+            eigenvectors(r, k) = std::complex<double>(vec[(size_t)k * O.rows() + r], 0.0);
     }
     return vals;
 }
@@ -326,7 +235,7 @@ Eigen::VectorXcd Op::IRLM_eigen(Eigen::SparseMatrix<double> O, int nb_eigen, Eig
 Eigen::VectorXd Op::FOLM_eigen(Eigen::SparseMatrix<double> O, int nb_iter, Eigen::MatrixXd& eigenvectors) {
     const int nev = std::max(1, std::min<int>({nb_iter, (int)O.rows() - 2, 32}));
     std::vector<double> ev, vec;
-    bhgb::eigsh(O, nev, ev, vec);
+    bhgb::eigsh(bhgb::csr_of(O), nev, ev, vec);
     Eigen::VectorXd vals(nev);
     eigenvectors.resize(O.rows(), nev);
     for (int k = 0; k < nev; ++k) {
