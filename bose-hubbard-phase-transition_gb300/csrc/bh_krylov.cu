@@ -1200,6 +1200,17 @@ static double keep_fraction() {
     return v;
 }
 
+// BH_TC_ROTATE=0: the restart rotation of the FP32 basis on the SIMT pipes
+// instead of the tensor cores
+static bool tc_rotation_on() {
+    static int v = -1;
+    if (v < 0) {
+        const char* e = std::getenv("BH_TC_ROTATE");
+        v = (e && *e == '0') ? 0 : 1;
+    }
+    return v == 1;
+}
+
 static bool debug_ortho() {
     static int v = -1;
     if (v < 0) {
@@ -1279,6 +1290,7 @@ struct Launcher {
     const OpView<T>& op;
     cudaStream_t st;
     int64_t* launches;
+    int* tc_status = nullptr;  // error flag of the tensor-core rotation (device)
 
     void done(const char* name, double bytes) const {
         const cudaError_t e = cudaGetLastError();
@@ -1451,6 +1463,18 @@ struct Launcher {
                 const T* Yg, const int* in_idx, const int* out_idx, T* Vout, int64_t ostride,
                 int ld_out, int single) const {
         if (Sproc <= 0) return;
+        if constexpr (std::is_same<T, float>::value) {
+            // FP32 basis: the tensor-core rotation (bh_rotate_tc.cu) where its
+            // shapes allow, else the SIMT kernel below
+            if (tc_rotation_on()) {
+                profile_begin(st);
+                if (rotate_tc(op.D, Sproc, ld_in, p, kc, nout, bstride, V, Yg, in_idx, out_idx, Vout, ostride,
+                              ld_out, single, tc_status, st)) {
+                    done("k_rotate_tc", (double)op.D * Sproc * p * ((double)kc / p + (double)nout / p) * sizeof(T));
+                    return;
+                }
+            }
+        }
         constexpr int V4 = 16 / sizeof(T), E = 128 / sizeof(T);
         // outputs per pass (a template value below); Y rows padded to a whole
         // number of passes so that every pass reads inside its row
@@ -1593,6 +1617,9 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
     const int kmax = rq.kmax, nb = kmax / p, Tdim = kmax + p;
     const int64_t bmax = D * (int64_t)S0 * p;
     Launcher<T> L{op, st, &res.launches};
+    DevBuf<int> tc_status(1);
+    BH_CUDA(cudaMemsetAsync(tc_status.p, 0, sizeof(int), st));
+    L.tc_status = tc_status.p;
     const int kcap = Tdim;
     int nch_max = 0, nchu_max = 0;
     for (int S = 1; S <= S0; ++S) {
@@ -2036,7 +2063,10 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
         ++restarts;
     }
     res.restarts = restarts;
+    int tc_err = 0;
+    BH_CUDA(cudaMemcpyAsync(&tc_err, tc_status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     BH_CUDA(cudaStreamSynchronize(st));
+    if (tc_err) throw Error(BH_ERR_TIMEOUT, "tensor-core rotation: a bounded mbarrier wait ran out");
 }
 
 void apply_operator(const OpView<double>& op, int ncols, int group, const double* d_prm,

@@ -253,6 +253,15 @@ void apply_operator_raw(const OpView<double>& op, int ncols, int group, const do
                         const double* d_X, double* d_Y, cudaStream_t st);
 
 // op64 must be set; op32 must be set for BH_PREC_MIXED (same pattern).
+// The thick-restart rotation of an FP32 basis on the tensor cores
+// (bh_rotate_tc.cu), same arguments and result as the SIMT rotation; false
+// (nothing launched) where its shapes do not fit (more than 256 outputs, block
+// size above 4, shared memory); *d_status (device) is set if a bounded wait
+// of a CTA ran out.
+bool rotate_tc(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t bstride, const float* V,
+               const float* Yg, const int* in_idx, const int* out_idx, float* Vout, int64_t ostride,
+               int ld_out, int single, int* d_status, cudaStream_t st);
+
 SolveResult block_lanczos(const OpView<double>& op64, const OpView<float>& op32,
                           const SolveRequest& rq, cudaStream_t st);
 
