@@ -647,10 +647,13 @@ int bh_phase_map(int m, int n_lo, int nsec, int nJ, const double* e0, int nmu, c
 }
 
 // ---- launch shapes of the sparse product and the autotuner ----
+// cols_per_lane < 0 in the C ABI: -VW adjacent columns per lane (the
+// contiguous-column product)
 static SpmmShape shape_in(const bh_spmm_shape& s) {
     SpmmShape o;
     o.L = s.lanes;
-    o.CW = s.cols_per_lane;
+    o.CW = s.cols_per_lane > 0 ? s.cols_per_lane : 0;
+    o.VW = s.cols_per_lane < 0 ? -s.cols_per_lane : 0;
     o.grid = s.grid;
     return o;
 }
@@ -658,7 +661,7 @@ static SpmmShape shape_in(const bh_spmm_shape& s) {
 static bh_spmm_shape shape_out(const SpmmShape& s) {
     bh_spmm_shape o;
     o.lanes = s.L;
-    o.cols_per_lane = s.CW;
+    o.cols_per_lane = s.VW > 0 ? -s.VW : s.CW;
     o.grid = s.grid;
     return o;
 }

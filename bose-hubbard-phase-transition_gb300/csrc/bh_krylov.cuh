@@ -129,6 +129,7 @@ struct SolveResult {
 struct SpmmShape {
     int L = 0, CW = 0;
     int64_t grid = 0;
+    int VW = 0;  // > 0: L lanes per row, each VW adjacent columns per pass (k_spmm_v)
 };
 
 // The matrix-free product also has a warp-per-row kernel (L = 32 at any
@@ -139,8 +140,11 @@ struct SpmmShape {
 // dl >= 1 the per-lane kernels from lmax, or 16 when lmax = 32, down), CW = 1
 // if narrow (else the widest that covers the lane's columns in few passes),
 // grid default or one wave.
+// vec = 1 (stored CSR, even ncols): the contiguous-column product k_spmm_v,
+// VW = 4 adjacent columns per lane (2 when ncols is not a multiple of 4) on
+// L = (the power of two >= ncols / VW, at most 32) >> dl lanes per row.
 struct SpmmChoice {
-    int dl = 0, narrow = 0, wave = 0;
+    int dl = 0, narrow = 0, wave = 0, vec = 0;
 };
 
 // Largest power of two <= 32 dividing ncols (the default lanes per row).
@@ -154,6 +158,11 @@ bool spmm_shape_valid(const SpmmShape& s, int ncols, bool matrix_free = false);
 // Whether the default product fuses the local coefficient (CSR with dpart,
 // block 2 or 4, one pass over the row's columns).
 bool spmm_fuses(bool matrix_free, bool has_dpart, int ncols, int group);
+// Columns per lane of the contiguous-column product at ncols (4, 2, or 0 when
+// ncols is odd), and whether the fused product uses it (one pass, whole
+// solves in every lane's columns).
+int spmm_vec_width(int ncols);
+bool spmm_fuses_vec(int ncols, int group);
 // Automatic tuning at first use (off with BH_AUTOTUNE=0).
 bool autotune_on();
 

@@ -36,6 +36,7 @@ constexpr int TC_M = 128;   // rows per tile = tensor-memory lanes
 constexpr int TC_KS = 8;    // TF32 values per MMA K-step (32 bytes)
 constexpr int TC_PIECES = 3;
 constexpr unsigned TC_SPIN = 1u << 24;  // polls of an mbarrier before giving up
+constexpr int TC_HEADER = 128;          // bytes of dynamic shared memory before the tiles
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -109,7 +110,9 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 
 }  // namespace
 
-// Shared memory: B[g][piece][ks] tiles of npad rows (all K-steps of the CTA's
+// Shared memory (all dynamic, so that the launch may take the device's
+// opt-in maximum): a 128-byte header (the two mbarriers, the tensor-memory
+// address), B[g][piece][ks] tiles of npad rows (all K-steps of the CTA's
 // coefficient matrices), then A[stage][g][piece] tiles of 128 rows.
 __global__ void __launch_bounds__(128)
 k_rotate_tc(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t bstride,
@@ -117,15 +120,15 @@ k_rotate_tc(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t bs
             const int* __restrict__ out_idx, float* __restrict__ Vout, int64_t ostride, int ld_out,
             int single, int G, int npad, int nks, int tmem_cols, int64_t rows_per_cta,
             int* __restrict__ status) {
-    extern __shared__ __align__(1024) unsigned char s_tc[];
-    __shared__ uint32_t s_tmem;
-    __shared__ __align__(8) uint64_t s_bar[2];
+    extern __shared__ __align__(128) unsigned char s_tc[];
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tc);
+    uint32_t& s_tmem = *reinterpret_cast<uint32_t*>(s_tc + 16);
     const int tid = threadIdx.x, warp = tid >> 5;
     const int sg0 = blockIdx.x * G;
     const int nsg = min(G, Sproc - sg0);
     const size_t btile = (size_t)npad * 32, atile = (size_t)TC_M * 32;
-    unsigned char* sB = s_tc;
-    unsigned char* sA = s_tc + (size_t)G * TC_PIECES * nks * btile;
+    unsigned char* sB = s_tc + TC_HEADER;
+    unsigned char* sA = sB + (size_t)G * TC_PIECES * nks * btile;
     const uint32_t bar0 = smem_u32(&s_bar[0]), bar1 = smem_u32(&s_bar[1]);
 
     if (tid == 0) {
@@ -167,66 +170,84 @@ k_rotate_tc(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t bs
 
     const int64_t r0 = (int64_t)blockIdx.y * rows_per_cta;
     const int64_t r1 = min(D, r0 + rows_per_cta);
-    uint32_t q = 0;  // global K-step counter of this CTA
-    bool ok = true;
-    for (int64_t t0 = r0; t0 < r1 && ok; t0 += TC_M) {
+    const int64_t nstep = r1 > r0 ? (r1 - r0 + TC_M - 1) / TC_M * nks : 0;
+    // the values of one K-step of this thread's row, loaded one step ahead so
+    // that their latency overlaps the current step's stores and products
+    float xr[4][TC_KS];
+    auto load_step = [&](int64_t step) {
+        const int64_t t0 = r0 + (step / nks) * TC_M;
+        const int ks = (int)(step % nks);
         const int64_t row = t0 + tid;
         const bool live = row < r1;
         const float* vrow = V + (live ? row : t0) * (int64_t)ld_in;
-        for (int ks = 0; ks < nks; ++ks, ++q) {
-            const int stage = q & 1;
-            const uint32_t bar = stage ? bar1 : bar0;
-            // the products of step q - 2 read this stage: wait for them (every
-            // thread polls; the CTA goes on only if all saw the arrival)
-            if (q >= 2 && !__syncthreads_and(mbar_wait(bar, ((q - 2) >> 1) & 1) ? 1 : 0)) {
-                ok = false;
-                break;
-            }
-            unsigned char* aS = sA + (size_t)stage * G * TC_PIECES * atile;
-#pragma unroll 1
-            for (int g = 0; g < G; ++g) {
-                unsigned char* ab = aS + (size_t)g * TC_PIECES * atile;
 #pragma unroll
-                for (int kk = 0; kk < TC_KS; ++kk) {
-                    const int c = ks * TC_KS + kk;
-                    const float x = (live && g < nsg && c < kc)
-                                        ? vrow[(int64_t)(c / p) * bstride + (int64_t)sin[g] * p + c % p]
-                                        : 0.f;
-                    float x0, x1, x2;
-                    split3(x, x0, x1, x2);
-                    const uint32_t off = tile_off(tid, kk);
-                    *reinterpret_cast<float*>(ab + off) = x0;
-                    *reinterpret_cast<float*>(ab + atile + off) = x1;
-                    *reinterpret_cast<float*>(ab + 2 * atile + off) = x2;
-                }
-            }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            __syncthreads();
-            if (tid == 0) {
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                for (int g = 0; g < nsg; ++g) {
-                    const uint32_t a0 = smem_u32(aS + (size_t)g * TC_PIECES * atile);
-                    const uint32_t b0 = smem_u32(sB + ((size_t)(g * TC_PIECES) * nks + ks) * btile);
-                    const uint32_t bstep = (uint32_t)(nks * btile), astep = (uint32_t)atile;
-                    const uint32_t d = tmem + (uint32_t)(g * npad);
-                    // (A piece, B piece): x0 y0, x0 y1, x1 y0, x0 y2, x1 y1, x2 y0
-                    const int pa[6] = {0, 0, 1, 0, 1, 2}, pb[6] = {0, 1, 0, 2, 1, 0};
+        for (int g = 0; g < 4; ++g)
 #pragma unroll
-                    for (int k = 0; k < 6; ++k)
-                        mma_tf32(d, tile_desc(a0 + pa[k] * astep), tile_desc(b0 + pb[k] * bstep), idesc,
-                                 (ks > 0 || k > 0) ? 1u : 0u);
-                }
-                mma_commit(bar);
+            for (int kk = 0; kk < TC_KS; ++kk) {
+                const int c = ks * TC_KS + kk;
+                xr[g][kk] = (g < nsg && live && c < kc)
+                                ? vrow[(int64_t)(c / p) * bstride + (int64_t)sin[g] * p + c % p]
+                                : 0.f;
+            }
+    };
+    if (nstep > 0) load_step(0);
+    uint32_t q = 0;  // K-steps whose products were committed
+    bool ok = true;
+    for (int64_t step = 0; step < nstep; ++step) {
+        const int ks = (int)(step % nks);
+        const int stage = (int)(step & 1);
+        const uint32_t bar = stage ? bar1 : bar0;
+        // the products of step - 2 read this stage: wait for them (every
+        // thread polls; the CTA goes on only if all saw the arrival)
+        if (step >= 2 && !__syncthreads_and(mbar_wait(bar, (uint32_t)((step - 2) >> 1) & 1) ? 1 : 0)) {
+            ok = false;
+            break;
+        }
+        unsigned char* aS = sA + (size_t)stage * G * TC_PIECES * atile;
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+            if (g >= G) break;
+            unsigned char* ab = aS + (size_t)g * TC_PIECES * atile;
+#pragma unroll
+            for (int kk = 0; kk < TC_KS; ++kk) {
+                float x0, x1, x2;
+                split3(xr[g][kk], x0, x1, x2);
+                const uint32_t off = tile_off(tid, kk);
+                *reinterpret_cast<float*>(ab + off) = x0;
+                *reinterpret_cast<float*>(ab + atile + off) = x1;
+                *reinterpret_cast<float*>(ab + 2 * atile + off) = x2;
             }
         }
-        if (!ok) break;
-        // the tile's products are complete once the last step's commit arrives
-        const uint32_t ql = q - 1;
-        if (!__syncthreads_and(mbar_wait((ql & 1) ? bar1 : bar0, (ql >> 1) & 1) ? 1 : 0)) {
+        if (step + 1 < nstep) load_step(step + 1);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            for (int g = 0; g < nsg; ++g) {
+                const uint32_t a0 = smem_u32(aS + (size_t)g * TC_PIECES * atile);
+                const uint32_t b0 = smem_u32(sB + ((size_t)(g * TC_PIECES) * nks + ks) * btile);
+                const uint32_t bstep = (uint32_t)(nks * btile), astep = (uint32_t)atile;
+                const uint32_t d = tmem + (uint32_t)(g * npad);
+                // (A piece, B piece): x0 y0, x0 y1, x1 y0, x0 y2, x1 y1, x2 y0
+                mma_tf32(d, tile_desc(a0), tile_desc(b0), idesc, ks > 0 ? 1u : 0u);
+                mma_tf32(d, tile_desc(a0), tile_desc(b0 + bstep), idesc, 1u);
+                mma_tf32(d, tile_desc(a0 + astep), tile_desc(b0), idesc, 1u);
+                mma_tf32(d, tile_desc(a0), tile_desc(b0 + 2 * bstep), idesc, 1u);
+                mma_tf32(d, tile_desc(a0 + astep), tile_desc(b0 + bstep), idesc, 1u);
+                mma_tf32(d, tile_desc(a0 + 2 * astep), tile_desc(b0), idesc, 1u);
+            }
+            mma_commit(bar);
+        }
+        q = (uint32_t)step + 1;
+        if (ks != nks - 1) continue;
+        // end of a tile: its products are complete once this step's commit arrives
+        if (!__syncthreads_and(mbar_wait(bar, (uint32_t)(step >> 1) & 1) ? 1 : 0)) {
             ok = false;
             break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int64_t row = r0 + (step / nks) * TC_M + tid;
+        const bool live = row < r1;
         for (int g = 0; g < nsg; ++g) {
             for (int c0 = 0; c0 < npad; c0 += 16) {
                 float v[16];
@@ -271,7 +292,7 @@ bool rotate_tc(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t
     BH_CUDA(cudaGetDevice(&dev));
     BH_CUDA(cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     auto smem_of = [&](int g) {
-        return (size_t)g * TC_PIECES * nks * npad * 32 + (size_t)2 * g * TC_PIECES * TC_M * 32;
+        return (size_t)TC_HEADER + (size_t)g * TC_PIECES * nks * npad * 32 + (size_t)2 * g * TC_PIECES * TC_M * 32;
     };
     while (G > 1 && smem_of(G) > (size_t)smax) G /= 2;
     size_t smem = smem_of(G);

@@ -148,6 +148,159 @@ k_spmm(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
     }
 }
 
+// Contiguous VW-column vectors of a row (16-byte aligned when the row's
+// offset is a multiple of VW columns and VW * sizeof(T) >= 16, else 8-byte).
+template <class T, int VW>
+struct SpVec {
+    T v[VW];
+};
+template <class T, int VW>
+__device__ __forceinline__ SpVec<T, VW> sp_ldv(const T* __restrict__ p) {
+    SpVec<T, VW> o;
+    if constexpr (std::is_same<T, float>::value && VW == 4) {
+        const float4 x = *reinterpret_cast<const float4*>(p);
+        o.v[0] = x.x, o.v[1] = x.y, o.v[2] = x.z, o.v[3] = x.w;
+    } else if constexpr (std::is_same<T, float>::value && VW == 2) {
+        const float2 x = *reinterpret_cast<const float2*>(p);
+        o.v[0] = x.x, o.v[1] = x.y;
+    } else {
+#pragma unroll
+        for (int q = 0; q < VW; q += 2) {
+            const double2 x = *reinterpret_cast<const double2*>(p + q);
+            o.v[q] = x.x, o.v[q + 1] = x.y;
+        }
+    }
+    return o;
+}
+template <class T, int VW>
+__device__ __forceinline__ void sp_stv(T* __restrict__ p, const SpVec<T, VW>& o) {
+    if constexpr (std::is_same<T, float>::value && VW == 4) {
+        *reinterpret_cast<float4*>(p) = make_float4(o.v[0], o.v[1], o.v[2], o.v[3]);
+    } else if constexpr (std::is_same<T, float>::value && VW == 2) {
+        *reinterpret_cast<float2*>(p) = make_float2(o.v[0], o.v[1]);
+    } else {
+#pragma unroll
+        for (int q = 0; q < VW; q += 2) *reinterpret_cast<double2*>(p + q) = make_double2(o.v[q], o.v[q + 1]);
+    }
+}
+
+// CSR product with contiguous column vectors: VL lanes per row, lane l
+// computes the VW adjacent columns t = VW (l + VL u) (u = pass; masked by
+// t < ncols, ncols a multiple of VW), so every gathered X row is read with
+// VW-wide vector loads and a warp's loads of one entry cover VL * VW
+// contiguous values.  Each column's sum is the same chain of fma_rn over the
+// row's entries in storage order as in k_spmm (four entries' rows requested
+// before their products), and the epilogue is the same: Y equals k_spmm's
+// bit for bit.  DP > 0 (block size, DP dividing VW, one pass over the row):
+// the lane's VW columns hold whole solves, so the partials of X_s^T Y_s need
+// no data from other lanes; FP32 sums over 16 rows, then FP64 slots in shared
+// memory, reduced per CTA into dpart[(cta DP + q) ncols + t] like k_spmm.
+template <class T, int VL, int VW, int DP>
+__global__ void __launch_bounds__(256)
+k_spmm_v(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
+         const T* __restrict__ X, T* __restrict__ Y, double* __restrict__ dpart) {
+    extern __shared__ double s_dot[];
+    const int gl = threadIdx.x % VL;
+    const int rows_per_block = blockDim.x / VL;
+    const int npass = (ncols + VL * VW - 1) / (VL * VW);
+    constexpr int NDP = DP > 0 ? DP : 1;
+    T dacc[VW][NDP];
+    int drows = 0;
+    if constexpr (DP > 0) {
+#pragma unroll
+        for (int v = 0; v < VW; ++v)
+#pragma unroll
+            for (int q = 0; q < NDP; ++q) {
+                dacc[v][q] = T(0);
+                s_dot[(size_t)(v * NDP + q) * blockDim.x + threadIdx.x] = 0.0;
+            }
+    }
+    for (int64_t r = (int64_t)blockIdx.x * rows_per_block + threadIdx.x / VL; r < A.D;
+         r += (int64_t)gridDim.x * rows_per_block) {
+        const int64_t e0 = A.rp[r], e1 = A.rp[r + 1];
+        const T d = A.vd ? A.vd[r] : T(0);
+        for (int u = 0; u < npass; ++u) {
+            const int t0 = (gl + VL * u) * VW;
+            const bool on = t0 < ncols;
+            T acc[VW];
+#pragma unroll
+            for (int v = 0; v < VW; ++v) acc[v] = T(0);
+            int64_t e = e0;
+            for (; e + 4 <= e1; e += 4) {
+                int64_t cc[4];
+                T vv[4];
+                SpVec<T, VW> xv[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    cc[k] = A.ci[e + k];
+                    vv[k] = A.tv[e + k];
+                }
+                if (on) {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) xv[k] = sp_ldv<T, VW>(X + cc[k] * ncols + t0);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+#pragma unroll
+                        for (int v = 0; v < VW; ++v) acc[v] = fma_rn(vv[k], xv[k].v[v], acc[v]);
+                }
+            }
+            for (; e < e1; ++e) {
+                const int64_t col = A.ci[e];
+                const T w = A.tv[e];
+                if (on) {
+                    const SpVec<T, VW> x = sp_ldv<T, VW>(X + col * ncols + t0);
+#pragma unroll
+                    for (int v = 0; v < VW; ++v) acc[v] = fma_rn(w, x.v[v], acc[v]);
+                }
+            }
+            if (!on) continue;
+            const SpVec<T, VW> xs = sp_ldv<T, VW>(X + r * ncols + t0);
+            SpVec<T, VW> yv;
+#pragma unroll
+            for (int v = 0; v < VW; ++v) {
+                const int s = (t0 + v) / group;
+                const T Jc = (T)prm[3 * s], Uc = (T)prm[3 * s + 1], sh = (T)prm[3 * s + 2];
+                yv.v[v] = fma_rn(Jc, acc[v], mul_rn(fma_rn(Uc, d, sh), xs.v[v]));
+            }
+            sp_stv<T, VW>(Y + r * ncols + t0, yv);
+            if constexpr (DP > 0) {
+#pragma unroll
+                for (int v = 0; v < VW; ++v)
+#pragma unroll
+                    for (int q = 0; q < DP; ++q) dacc[v][q] += xs.v[(v / DP) * DP + q] * yv.v[v];
+            }
+        }
+        if constexpr (DP > 0) {
+            if (++drows == 16) {
+                drows = 0;
+#pragma unroll
+                for (int v = 0; v < VW; ++v)
+#pragma unroll
+                    for (int q = 0; q < NDP; ++q) {
+                        s_dot[(size_t)(v * NDP + q) * blockDim.x + threadIdx.x] += (double)dacc[v][q];
+                        dacc[v][q] = T(0);
+                    }
+            }
+        }
+    }
+    if constexpr (DP > 0) {
+#pragma unroll
+        for (int v = 0; v < VW; ++v)
+#pragma unroll
+            for (int q = 0; q < NDP; ++q)
+                s_dot[(size_t)(v * NDP + q) * blockDim.x + threadIdx.x] += (double)dacc[v][q];
+        __syncthreads();
+        for (int e = threadIdx.x; e < ncols * DP; e += blockDim.x) {
+            const int t = e / DP, q = e % DP;
+            const int g = t / VW, v = t % VW;
+            double sum = 0.0;
+            for (int ro = 0; ro < rows_per_block; ++ro)
+                sum += s_dot[(size_t)(v * NDP + q) * blockDim.x + ro * VL + g];
+            dpart[((size_t)blockIdx.x * DP + q) * ncols + t] = sum;
+        }
+    }
+}
+
 // Target index and amplitude of directed bond k of the state with index r,
 // occupations w and packed suffix sums sufp; c = -1 if site i is empty.
 template <class T>
@@ -460,6 +613,18 @@ int spmm_fused_per_sm() {
     return n;
 }
 
+// Resident CTAs per SM of the fused contiguous-column product (found once per instance).
+template <class T, int VL, int VW, int DP>
+int spmm_fused_v_per_sm() {
+    static std::atomic<int> occ{0};
+    int n = occ.load(std::memory_order_relaxed);
+    if (n == 0) {
+        n = std::max(1, resident_ctas(k_spmm_v<T, VL, VW, DP>, 256, (size_t)256 * VW * DP * sizeof(double)));
+        occ.store(n, std::memory_order_relaxed);
+    }
+    return n;
+}
+
 // Dynamic shared memory of the matrix-free product at L lanes per row: the
 // -sqrt table, the rank table and the bonds, plus (L >= 4) the hop lists of
 // the CTA's rows ((256 / L) rows x nbonds x (int32 + T), 16-byte aligned parts).
@@ -521,11 +686,44 @@ void by_shape(int L, int cw, F&& f) {
     }
 }
 
+// Calls f(VL, VW) as compile-time constants: VL in {2, 4, 8, 16, 32}, VW in {2, 4}.
+template <class F>
+void by_vshape(int VL, int VW, F&& f) {
+    auto w = [&](auto lc) {
+        if (VW == 2) f(lc, std::integral_constant<int, 2>());
+        else f(lc, std::integral_constant<int, 4>());
+    };
+    switch (VL) {
+        case 2: w(std::integral_constant<int, 2>()); break;
+        case 4: w(std::integral_constant<int, 4>()); break;
+        case 8: w(std::integral_constant<int, 8>()); break;
+        case 16: w(std::integral_constant<int, 16>()); break;
+        default: w(std::integral_constant<int, 32>()); break;
+    }
+}
+
 // The product without the fused partials, with shape s (L, CW from the
-// instantiated set: CW in {1, 4} for L < 32, {1, 2, 4} for L = 32).
+// instantiated set: CW in {1, 4} for L < 32, {1, 2, 4} for L = 32; or the
+// contiguous-column product when s.VW > 0).
 template <class T, bool MF>
 void spmm_launch_plain(const OpView<T>& op, int ncols, int group, const double* prm, const T* X, T* Y,
                        cudaStream_t st, const SpmmShape& s) {
+    if constexpr (!MF) {
+        if (s.VW > 0) {
+            const int64_t rows = (op.D + (256 / s.L) - 1) / (256 / s.L);
+            auto go = [&](auto lc, auto wc) {
+                constexpr int VL = decltype(lc)::value, VW = decltype(wc)::value;
+                auto kern = k_spmm_v<T, VL, VW, 0>;
+                int64_t g = s.grid;
+                if (g == 0) g = std::min<int64_t>(rows, (int64_t)sm_count() * 16);
+                else if (g < 0) g = std::min<int64_t>(rows, (int64_t)sm_count() * std::max(1, resident_ctas(kern, 256, 0)));
+                g = std::max<int64_t>(1, std::min<int64_t>(g, 0x7fffffff));
+                kern<<<(unsigned)g, 256, 0, st>>>(op, ncols, group, prm, X, Y, nullptr);
+            };
+            by_vshape(s.L, s.VW, go);
+            return;
+        }
+    }
     const int64_t rows = (op.D + (256 / s.L) - 1) / (256 / s.L);
     size_t smem = 0;
     if (MF) {
@@ -564,6 +762,32 @@ double launch_spmm_kind(const OpView<T>& op, int ncols, int group, const double*
     const SpmmShape def = spmm_resolve(SpmmChoice{}, ncols, MF);
     const int L = def.L, CW = def.CW;
     if (dparts) *dparts = 0;
+    if (!MF && dpart != nullptr && (group == 2 || group == 4) && spmm_fuses_vec(ncols, group)) {
+        // fused X^T Y partials on the contiguous-column product (every lane
+        // holds whole solves), one resident wave
+        const SpmmShape v = spmm_resolve(SpmmChoice{0, 0, 0, 1}, ncols, false);
+        const int rpb = 256 / v.L;
+        const int64_t g = std::max<int64_t>(1, std::min<int64_t>((D + rpb - 1) / rpb, (int64_t)sm_count() * 16));
+        auto go = [&](auto lc, auto wc) {
+            constexpr int VL = decltype(lc)::value, VW = decltype(wc)::value;
+            auto fused = [&](auto dpc) {
+                constexpr int DPP = decltype(dpc)::value;
+                if constexpr (VW % DPP == 0) {
+                    auto kern = k_spmm_v<T, VL, VW, DPP>;
+                    const size_t smem = (size_t)256 * VW * DPP * sizeof(double);
+                    const int per_sm = std::min(4, spmm_fused_v_per_sm<T, VL, VW, DPP>());
+                    const int64_t gf = std::min<int64_t>(g, (int64_t)sm_count() * per_sm);
+                    if (dparts) *dparts = (int)gf;
+                    allow_large_smem(kern, smem);
+                    kern<<<(unsigned)gf, 256, smem, st>>>(op, ncols, group, prm, X, Y, dpart);
+                }
+            };
+            if (group == 2) fused(std::integral_constant<int, 2>());
+            else fused(std::integral_constant<int, 4>());
+        };
+        if constexpr (!MF) by_vshape(v.L, v.VW, go);
+        return spmm_bytes<T, MF>(op, ncols);
+    }
     if (spmm_fuses(MF, dpart != nullptr, ncols, group)) {
         // fused X^T Y partials (CSR, one pass over the columns, block size 2
         // or 4) on one resident wave (fewer partial rows to reduce, no tail wave)

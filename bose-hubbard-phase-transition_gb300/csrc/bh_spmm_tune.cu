@@ -32,8 +32,25 @@ static int wide_cw(int L, int cpl) {
     return 4;
 }
 
+// Lanes per row of the contiguous-column product at ncols with VW columns
+// per lane (one pass when ncols <= 32 VW).
+static int vec_lanes(int ncols, int vw) {
+    int L = 2;
+    while (L < 32 && L * vw < ncols) L *= 2;
+    return L;
+}
+
+int spmm_vec_width(int ncols) { return ncols % 4 == 0 ? 4 : (ncols % 2 == 0 ? 2 : 0); }
+
 SpmmShape spmm_resolve(const SpmmChoice& c, int ncols, bool matrix_free) {
     SpmmShape s;
+    if (c.vec && !matrix_free) {
+        s.VW = spmm_vec_width(ncols);
+        s.L = std::max(2, vec_lanes(ncols, s.VW) >> c.dl);
+        s.CW = 0;
+        s.grid = c.wave ? -1 : 0;
+        return s;
+    }
     const int lmax = spmm_lmax(ncols);
     int L, cpl;
     if (matrix_free && c.dl == 0) {
@@ -69,19 +86,43 @@ std::vector<SpmmChoice> spmm_candidates(int ncols, bool matrix_free) {
                 out.push_back(c);
             }
         }
+    // stored CSR at even widths of at least 4: the contiguous-column product
+    // on the lanes that cover the row in one pass, and half as many
+    if (!matrix_free && ncols >= 4 && spmm_vec_width(ncols) > 0) {
+        std::vector<std::tuple<int, int64_t>> vseen;
+        for (int wave = 0; wave < 2; ++wave)
+            for (int dl = 0; dl < 2; ++dl) {
+                const SpmmChoice c{dl, 0, wave, 1};
+                const SpmmShape s = spmm_resolve(c, ncols, false);
+                const auto t = std::make_tuple(s.L, s.grid);
+                if (std::find(vseen.begin(), vseen.end(), t) != vseen.end()) continue;
+                vseen.push_back(t);
+                out.push_back(c);
+            }
+    }
     return out;
 }
 
 bool spmm_shape_valid(const SpmmShape& s, int ncols, bool matrix_free) {
     if (ncols < 1 || s.grid < -1) return false;
+    if (s.VW != 0) {
+        if (matrix_free || !(s.VW == 2 || s.VW == 4) || ncols % s.VW != 0) return false;
+        return s.L == 2 || s.L == 4 || s.L == 8 || s.L == 16 || s.L == 32;
+    }
     if (!(s.L == 1 || s.L == 2 || s.L == 4 || s.L == 8 || s.L == 16 || s.L == 32)) return false;
     if (!(s.CW == 1 || s.CW == 4 || (s.CW == 2 && s.L == 32))) return false;
     if (matrix_free && s.L == 32) return true;  // warp per row, masked columns
     return ncols % s.L == 0;
 }
 
+bool spmm_fuses_vec(int ncols, int group) {
+    const int vw = spmm_vec_width(ncols);
+    return vw > 0 && vw % group == 0 && ncols >= 4 && vec_lanes(ncols, vw) * vw >= ncols;
+}
+
 bool spmm_fuses(bool matrix_free, bool has_dpart, int ncols, int group) {
     if (matrix_free || !has_dpart || !(group == 2 || group == 4) || ncols < 1) return false;
+    if (spmm_fuses_vec(ncols, group)) return true;
     const SpmmShape d = spmm_resolve(SpmmChoice{}, ncols, false);
     return ncols / d.L <= d.CW && d.L >= group;
 }

@@ -312,7 +312,10 @@ int bh_profile_get(int i, char* name, int name_cap, int64_t* launches, double* m
 /* matrix-free product also runs one warp per row, lanes = 32, at any      */
 /* nvec, its default),                                                     */
 /* `cols_per_lane` columns per thread per pass (1 or 4, also 2 with 32     */
-/* lanes) on `grid` CTAs of 256 threads striding over the rows (0: the     */
+/* lanes; for stored CSR also -4 or -2: that many ADJACENT columns per     */
+/* lane, read as one vector, on 2..32 lanes per row, columns masked, any   */
+/* width that is a multiple of 4 or 2)                                     */
+/* on `grid` CTAs of 256 threads striding over the rows (0: the            */
 /* default min(rows / (256 / lanes), 16 per SM); -1: one resident wave).   */
 /* Every shape gives the same y bit for bit.  The solvers time the         */
 /* candidate shapes the first time a width class of an operator is seen    */

@@ -1,10 +1,11 @@
 """CPU: the launch shapes the autotuner of the sparse product chooses from.
 
 Every candidate must be a shape the library has a kernel for (lanes a power of
-two <= 32 dividing the width, 1 or 4 columns per lane, 2 only with 32 lanes),
-the default shape must come first and equal the fixed rule the product used
-before it had a tuner, and no shape may repeat.  No GPU is touched: these are
-host-only entry points."""
+two <= 32 dividing the width, 1 or 4 columns per lane, 2 only with 32 lanes;
+or, for stored CSR at even widths, -4 / -2: that many adjacent columns per
+lane on 2..32 lanes), the default shape must come first and equal the fixed
+rule the product used before it had a tuner, and no shape may repeat.  No GPU
+is touched: these are host-only entry points."""
 import ctypes as C
 
 import pytest
@@ -30,11 +31,17 @@ def test_candidates_valid_default_first_unique(pkg, nvec):
     cands = pkg.spmm_candidates(nvec)
     assert cands[0] == default_shape(nvec)
     assert len(set(cands)) == len(cands)
-    assert 1 <= len(cands) <= 12
+    assert 1 <= len(cands) <= 16
     for lanes, cw, grid in cands:
-        assert lanes in (1, 2, 4, 8, 16, 32) and nvec % lanes == 0
-        assert cw in (1, 4) or (cw == 2 and lanes == 32)
+        if cw < 0:  # contiguous columns: -cw adjacent columns per lane, masked
+            assert cw in (-2, -4) and nvec % -cw == 0 and nvec >= 4
+            assert lanes in (2, 4, 8, 16, 32)
+        else:
+            assert lanes in (1, 2, 4, 8, 16, 32) and nvec % lanes == 0
+            assert cw in (1, 4) or (cw == 2 and lanes == 32)
         assert grid in (0, -1)
+    # the contiguous-column shapes exist exactly at even widths >= 4
+    assert any(c[1] < 0 for c in cands) == (nvec >= 4 and nvec % 2 == 0)
     # both grid rules for the default lane count
     assert (cands[0][0], cands[0][1], -1) in cands
 
@@ -54,11 +61,15 @@ def test_matrix_free_candidates(pkg, nvec):
 
 def test_candidates_cover_fewer_lanes(pkg):
     cands = pkg.spmm_candidates(128)
-    lanes = {c[0] for c in cands}
+    lanes = {c[0] for c in cands if c[1] > 0}
     assert lanes == {32, 16, 8}
-    # odd multiples of two (batches with an odd number of block-2 solves)
-    lanes = {c[0] for c in pkg.spmm_candidates(126)}
-    assert lanes == {2, 1}
+    assert {c[0] for c in cands if c[1] < 0} == {32, 16} and all(c[1] == -4 for c in cands if c[1] < 0)
+    # odd multiples of two (batches with an odd number of block-2 solves):
+    # 1 or 2 lanes per row with strided columns, or 32 / 16 lanes with two
+    # adjacent columns each
+    cands = pkg.spmm_candidates(126)
+    assert {c[0] for c in cands if c[1] > 0} == {2, 1}
+    assert {(c[0], c[1]) for c in cands if c[1] < 0} == {(32, -2), (16, -2)}
 
 
 def test_candidates_argument_errors(pkg):

@@ -54,6 +54,12 @@ def test_every_shape_gives_the_default_product_bit_for_bit(pkg, prec):
             if h.matrix_free:
                 # the warp-per-row kernel at every column width, one and several passes
                 shapes += [(32, 1, 0), (32, 2, 5), (32, 4, -1)]
+            else:
+                # the contiguous-column product: several passes per lane, odd grids
+                if nvec % 2 == 0:
+                    shapes += [(2, -2, 0), (32, -2, -1), (4, -2, 5)]
+                if nvec % 4 == 0:
+                    shapes += [(2, -4, 3), (8, -4, 0)]
             for s in shapes:
                 y = h.apply_shape(x, 0.11, 1.0, 0.3, s, precision=p)
                 assert np.array_equal(y, y0), (name, nvec, s)
@@ -62,7 +68,8 @@ def test_every_shape_gives_the_default_product_bit_for_bit(pkg, prec):
 def test_shape_arguments_are_checked(pkg):
     h = pkg.Hamiltonian(pkg.Basis(4, 3), chain_lists(4))
     x = np.ones((h.D, 6))
-    for bad in [(4, 4, 0), (3, 1, 0), (2, 2, 0), (2, 4, -2), (64, 1, 0)]:
+    for bad in [(4, 4, 0), (3, 1, 0), (2, 2, 0), (2, 4, -2), (64, 1, 0), (32, -4, 0), (3, -2, 0),
+                (64, -2, 0), (4, -3, 0)]:
         with pytest.raises(ValueError, match="launch shape"):
             h.apply_shape(x, 0.1, 1.0, 0.0, bad)
 
