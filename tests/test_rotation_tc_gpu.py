@@ -3,7 +3,10 @@ cores (tcgen05.mma kind::tf32 with three-piece TF32 splits, bh_rotate_tc.cu)
 against the SIMT rotation (BH_TC_ROTATE=0, run in a child process because the
 switch is read once per process).  Both solves must give the FP64 path's
 eigenvalues within 1e-8 (pure relative), for block sizes 1, 2 and 4 (the
-tensor-core kernel's three layouts of a basis row)."""
+tensor-core kernel's three layouts of a basis row).  Block 1 runs on the open
+chain: the periodic chain's degenerate pairs need a block of 2 (one Krylov
+vector finds one copy of a pair, and FP32 rounding can add a spurious second
+copy that FP64 does not)."""
 import json
 import os
 import subprocess
@@ -20,7 +23,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 CASES = [  # (m, n, lattice, block, nJ, nev)
     (10, 9, "chain", 2, 32, 10),
-    (9, 7, "chain", 1, 8, 6),
+    (9, 7, "open", 1, 8, 6),
     (16, 5, "square", 4, 8, 4),
 ]
 
@@ -33,7 +36,10 @@ pkg = g.load_package(); pkg.load()
 out = []
 for m, n, lat, block, nj, nev in {cases!r}:
     nb = pkg.Neighbours(m)
-    (nb.chain_neighbours if lat == "chain" else nb.square_neighbours)()
+    if lat == "square":
+        nb.square_neighbours()
+    else:
+        nb.chain_neighbours(lat == "chain")
     h = pkg.Hamiltonian(pkg.Basis(m, n), nb.getNeighbours())
     Js = 0.3 * (np.arange(nj) + 1) / nj
     ev, _, nc, info = h.eigsh_batch(Js, 1.0, 0.0, nev=nev, block=block, precision=pkg.PREC_MIXED)
@@ -55,12 +61,15 @@ def test_tensor_core_rotation_matches_simt_and_fp64(pkg):
     simt = _solve_all("0")
     for (m, n, lat, block, nj, nev), a, b in zip(CASES, tc, simt):
         nb = pkg.Neighbours(m)
-        (nb.chain_neighbours if lat == "chain" else nb.square_neighbours)()
+        if lat == "square":
+            nb.square_neighbours()
+        else:
+            nb.chain_neighbours(lat == "chain")
         h = pkg.Hamiltonian(pkg.Basis(m, n), nb.getNeighbours())
         Js = 0.3 * (np.arange(nj) + 1) / nj
         ev64, _, nc64, _ = h.eigsh_batch(Js, 1.0, 0.0, nev=nev, block=block, precision=pkg.PREC_FP64)
         ea, eb = np.array(a["ev"]), np.array(b["ev"])
         assert min(a["nc"]) == nev and min(b["nc"]) == nev
-        for e in (ea, eb):
+        for name, e in (("tensor cores", ea), ("SIMT", eb)):
             rel = np.abs(e - ev64) / np.abs(ev64)
-            assert rel.max() < 1e-8, (m, n, block, rel.max())
+            assert rel.max() < 1e-8, (name, m, n, lat, block, rel.max())
