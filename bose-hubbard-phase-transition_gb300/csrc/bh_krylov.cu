@@ -562,18 +562,48 @@ k_qr_finalize(int p, int nchunks, int ncols, const double* __restrict__ gpart, i
               double* __restrict__ Tm, int Tdim, int jrow, double kill_abs,
               unsigned char* __restrict__ dead, int* __restrict__ need3) {
     __shared__ double G[16][16];
+    __shared__ double red[QR_THREADS / 32][16];
     const int s = blockIdx.x;
-    const int warp = threadIdx.x >> 5;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // final pass of a step whose blocks were all well conditioned: the middle
     // Gram pass was skipped and the block is already orthonormal (G = I)
     const bool skipped = mode == 2 && need3 && *need3 == 0;
-    for (int e = warp; e < p * p; e += QR_THREADS / 32) {
-        const int a = e / p, b = e % p;
-        const double v = skipped ? (a == b ? 1.0 : 0.0)
-                                 : warp_sum_chunks(gpart, nchunks, (size_t)p * ncols, (size_t)a * ncols + s * p + b);
-        if ((threadIdx.x & 31) == 0) G[a][b] = v;
+    // G = sum of the chunk partials: every thread sums the chunks
+    // tid, tid + QR_THREADS, ... of each entry (independent loads in flight),
+    // then a fixed-order reduction over the lanes and the warps
+    for (int e0 = 0; e0 < p * p; e0 += 16) {
+        const int ne = min(16, p * p - e0);
+        double acc[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) acc[k] = 0.0;
+        if (!skipped) {
+            for (int ch = threadIdx.x; ch < nchunks; ch += QR_THREADS) {
+                const double* gp = gpart + (size_t)ch * p * ncols;
+#pragma unroll
+                for (int k = 0; k < 16; ++k) {
+                    if (k < ne) {
+                        const int e = e0 + k, a = e / p, b = e % p;
+                        acc[k] += gp[(size_t)a * ncols + s * p + b];
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            double v = acc[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) red[warp][k] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < ne) {
+            const int e = e0 + threadIdx.x, a = e / p, b = e % p;
+            double v = 0.0;
+            for (int w = 0; w < QR_THREADS / 32; ++w) v += red[w][threadIdx.x];
+            G[a][b] = skipped ? (a == b ? 1.0 : 0.0) : v;
+        }
+        __syncthreads();
     }
-    __syncthreads();
     if (threadIdx.x != 0) return;
     double R[16][16], Ri[16][16], Rt[16][16];
     for (int a = 0; a < p; ++a)
@@ -1200,13 +1230,18 @@ static double keep_fraction() {
     return v;
 }
 
-// BH_TC_ROTATE=0: the restart rotation of the FP32 basis on the SIMT pipes
-// instead of the tensor cores
+// BH_TC_ROTATE=1: the restart rotation of the FP32 basis on the tensor cores
+// (bh_rotate_tc.cu) instead of the SIMT kernel.  Off by default: measured on
+// the m=10, n=10 sector (64 solves, block 2) it took 108.5 ms over 47
+// rotations against 23.0 ms for the SIMT kernel -- the exact three-piece TF32
+// split of every basis value costs as many instructions per value as the SIMT
+// kernel's FMAs, and one 132 KB CTA per SM leaves 4 warps to hide the loads
+// (ncu: tensor pipe 2.3% active, warps active 6.3%).
 static bool tc_rotation_on() {
     static int v = -1;
     if (v < 0) {
         const char* e = std::getenv("BH_TC_ROTATE");
-        v = (e && *e == '0') ? 0 : 1;
+        v = (e && *e == '1') ? 1 : 0;
     }
     return v == 1;
 }

@@ -1,7 +1,7 @@
 """GPU: the thick-restart rotation of the FP32 Krylov basis on the tensor
-cores (tcgen05.mma kind::tf32 with three-piece TF32 splits, bh_rotate_tc.cu)
-against the SIMT rotation (BH_TC_ROTATE=0, run in a child process because the
-switch is read once per process).  Both solves must give the FP64 path's
+cores (tcgen05.mma kind::tf32 with three-piece TF32 splits, bh_rotate_tc.cu,
+BH_TC_ROTATE=1) against the SIMT rotation (the default, BH_TC_ROTATE=0), each in
+a child process because the switch is read once per process.  Both solves must give the FP64 path's
 eigenvalues within 1e-8 (pure relative), for block sizes 1, 2 and 4 (the
 tensor-core kernel's three layouts of a basis row).  Block 1 runs on the open
 chain: the periodic chain's degenerate pairs need a block of 2 (one Krylov
