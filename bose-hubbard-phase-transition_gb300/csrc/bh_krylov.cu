@@ -116,9 +116,18 @@ k_dot(int64_t D, int ncols, int ld, int p, int nblk, int64_t bstride, const T* _
 __device__ __forceinline__ double warp_sum_chunks(const double* __restrict__ part, int nchunks,
                                                   size_t chunk_stride, size_t offset) {
     const int lane = threadIdx.x & 31;
-    double v = 0.0;
-#pragma unroll 4
-    for (int ch = lane; ch < nchunks; ch += 32) v += part[(size_t)ch * chunk_stride + offset];
+    // four independent partial sums per lane (chunks lane + 32 (4 i + k)), so
+    // that four loads are in flight; fixed order, so the result is deterministic
+    double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
+    int ch = lane;
+    for (; ch + 96 < nchunks; ch += 128) {
+        v0 += part[(size_t)ch * chunk_stride + offset];
+        v1 += part[(size_t)(ch + 32) * chunk_stride + offset];
+        v2 += part[(size_t)(ch + 64) * chunk_stride + offset];
+        v3 += part[(size_t)(ch + 96) * chunk_stride + offset];
+    }
+    for (; ch < nchunks; ch += 32) v0 += part[(size_t)ch * chunk_stride + offset];
+    double v = (v0 + v1) + (v2 + v3);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
