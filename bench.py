@@ -581,7 +581,9 @@ def run_extra(args):
     pkg.profile_enable(True)
     solve(pkg.PREC_MIXED, c["J"][:4])
     pkg.profile_enable(False)
-    roof, shares = _profile_summary(pkg, pkg.profile_read())
+    prof = pkg.profile_read()
+    roof, shares = _profile_summary(pkg, prof)
+    gather = _spmm_gather(prof, h, c["matrix_free"])
     out = {"metric": "eigensolves/s (batched mixed-precision, <=1e-8 rel err vs FP64)",
            "value": round(value, 4), "unit": "eigensolves/s", "n_gpus": 1, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(1e3 * sum(ts) / args.steps, 1),
@@ -595,8 +597,33 @@ def run_extra(args):
                         "points": [int(k) for k in smp]},
            "plain_fp64": {"value": round(len(smp) / t64, 5), "unit": "eigensolves/s",
                           "batched_mixed_over_plain": round(value / (len(smp) / t64), 2)},
-           "roofline": roof, "kernel_time_shares": shares, "clocks": clk}
+           "roofline": roof, "spmm_gather": gather, "kernel_time_shares": shares, "clocks": clk}
     print(json.dumps(out), flush=True)
+
+
+def _spmm_gather(prof, h, matrix_free):
+    """The sparse product against the bandwidth of the bytes it must gather.
+    The algorithmic count reads X once per product; every stored (or
+    regenerated) entry gathers one whole row of X (ncols values), so the
+    product moves  op + Z B s + 2 D B s  bytes (op: CSR pattern, values and
+    diagonal, or the packed occupations; Z off-diagonal entries; B columns;
+    s bytes per value), most of it from DRAM when X does not fit in L2.
+    The total B over the product's launches follows from its algorithmic
+    bytes, which are linear in B."""
+    name = "k_spmm_mf" if matrix_free else "k_spmm"
+    rec = prof.get(name)
+    if not rec or not rec["launches"]:
+        return None
+    s_val, D, Z, L = 4.0, float(h.D), float(h.nnz_offdiag), rec["launches"]
+    op = D * 8.0 if matrix_free else Z * (4.0 + s_val) + (D + 1.0) * 8.0 + D * s_val
+    sumB = (rec["bytes"] - L * op) / (2.0 * D * s_val)
+    gbytes = L * op + (Z + 2.0 * D) * s_val * sumB
+    peak, kind = measured_peaks()
+    achieved = gbytes / (rec["ms"] / 1e3) / 1e9
+    return {"kernel": name, "gather_bytes_per_launch": round(gbytes / L), "achieved": round(achieved, 1),
+            "peak": peak, "peak_kind": kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+            "mean_columns": round(sumB / L, 1),
+            "definition": "(operator bytes + entries x columns x 4 B + 2 x D x columns x 4 B) / CUDA-event time"}
 
 
 # E0 of the m=n=12 chain at J=0.05, U=1, mu=0.6 from the reference's Op::IRLM_eigen

@@ -71,7 +71,7 @@ EXPORTS = [
     "bh_neighbours_cube", "bh_dimension", "bh_basis_create", "bh_basis_destroy",
     "bh_basis_info", "bh_basis_copy", "bh_basis_index", "bh_hamiltonian_create",
     "bh_hamiltonian_create_matrix_free", "bh_hamiltonian_is_matrix_free",
-    "bh_hamiltonian_destroy", "bh_hamiltonian_nnz", "bh_hamiltonian_csr",
+    "bh_hamiltonian_destroy", "bh_hamiltonian_nnz", "bh_hamiltonian_csr", "bh_hamiltonian_multi_csr",
     "bh_hamiltonian_apply", "bh_hamiltonian_apply_noalloc", "bh_solver_opts_default", "bh_eigsh", "bh_eigsh_csr",
     "bh_eigsh_batch", "bh_eigsh_batch_status", "bh_eigsh_batch_vectors", "bh_eigsh_batch_sectors", "bh_dense_eigh", "bh_gap_ratios", "bh_spdm", "bh_phase_map", "bh_scmf", "bh_mean_field_grid", "bh_profile_enable",
     "bh_profile_reset", "bh_profile_count", "bh_profile_get",
@@ -110,6 +110,7 @@ def load() -> C.CDLL:
     L.bh_hamiltonian_destroy.argtypes = [vp]
     L.bh_hamiltonian_nnz.argtypes = [vp, i64p]
     L.bh_hamiltonian_csr.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, vp, vp, vp]
+    L.bh_hamiltonian_multi_csr.argtypes = [C.c_int, vp, C.c_int, C.c_double, C.c_double, C.c_double, vp, vp, vp]
     L.bh_hamiltonian_apply.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, vp, vp]
     L.bh_hamiltonian_apply_noalloc.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double,
                                                 C.c_int, vp, vp, vp]
@@ -397,6 +398,23 @@ def eigsh_sectors(hams, J, U, mu, nev: int = 10, **opt):
     return ev, rs, nc, _info(info)
 
 
+def multi_sector_csr(hams, J: float, U: float, mu: float, order: int = ORDER_REFERENCE):
+    """Block-diagonal H = J T + U V - mu N of several sector Hamiltonians,
+    assembled on the device (bh_hamiltonian_multi_csr), as scipy CSR."""
+    import scipy.sparse as sp
+
+    nh = len(hams)
+    D = sum(h.D for h in hams)
+    nz = sum(h.nnz_offdiag + h.D for h in hams)
+    rp = np.zeros(D + 1, np.int64)
+    ci = np.zeros(max(nz, 1), np.int32)
+    val = np.zeros(max(nz, 1), np.float64)
+    hs = (C.c_void_p * nh)(*[h._h.value for h in hams])
+    _check(load().bh_hamiltonian_multi_csr(nh, C.cast(hs, C.c_void_p), order, J, U, mu, _ptr(rp), _ptr(ci),
+                                           _ptr(val)))
+    return sp.csr_matrix((val[:nz], ci[:nz], rp), shape=(D, D))
+
+
 def _info(i: bh_solve_info) -> SolveInfo:
     return SolveInfo(i.nconv, i.restarts, i.matvecs, i.max_resid, i.seconds, i.launches)
 
@@ -592,11 +610,29 @@ class BH:
 
         n_min = max(0, n_min)
         n_max = max(n_max, n_min)
-        blocks = []
-        for bosons in range(n_min, n_max + 1):
-            tags, basis = BH.fixed_set_basis(m, bosons)
-            blocks.append(BH.fixed_bosons_hamiltonian(neighbours, basis, tags, m, bosons, J, U, mu))
-        return sp.block_diag(blocks, format="csr")
+        eps = np.finfo(float).eps
+        if abs(J) > eps:
+            terms = (J, 0.0, 0.0)
+        elif abs(U) > eps:
+            terms = (0.0, U, 0.0)
+        elif abs(mu) > eps:
+            terms = (0.0, 0.0, mu)
+        else:
+            import sys
+
+            for _ in range(n_min, n_max + 1):
+                print("Error: At least one of the parameters J, U, mu must be different from zero.",
+                      file=sys.stderr)
+            D = sum(BH.dimension(m, b) for b in range(n_min, n_max + 1))
+            return sp.csr_matrix((D, D))
+        hams = [Hamiltonian(Basis(m, b), neighbours) for b in range(n_min, n_max + 1)]
+        H = multi_sector_csr(hams, *terms)
+        if terms[0] != 0.0:
+            H.eliminate_zeros()  # hopping only: no diagonal entries, as fill_hopping
+            return H
+        d = H.diagonal()  # one explicit entry per row, as fill_interaction / fill_chemical
+        D = len(d)
+        return sp.csr_matrix((d, np.arange(D, dtype=np.int32), np.arange(D + 1)), shape=(D, D))
 
     @staticmethod
     def h_MF(psi: float, p: int, mu: float, J: float, q: int) -> np.ndarray:

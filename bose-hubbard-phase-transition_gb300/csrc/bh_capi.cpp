@@ -329,6 +329,31 @@ int bh_hamiltonian_csr(const bh_hamiltonian* h, int order, double J, double U, d
     });
 }
 
+int bh_hamiltonian_multi_csr(int nh, const bh_hamiltonian* const* hs, int order, double J, double U,
+                             double mu, int64_t* row_ptr, int32_t* col, double* val) {
+    return guard([&] {
+        BH_REQUIRE(nh >= 1 && hs && row_ptr && col && val, "null argument or nh < 1");
+        BH_REQUIRE(order == BH_ORDER_REFERENCE || order == BH_ORDER_LEX, "unknown order");
+        require_finite_params(J, U, mu);
+        int64_t D = 0, nz = 0;
+        for (int k = 0; k < nh; ++k) {
+            BH_REQUIRE(hs[k] != nullptr, "null Hamiltonian");
+            BH_REQUIRE(k == 0 || hs[k]->device == hs[0]->device, "Hamiltonians on different devices");
+            D += hs[k]->D;
+            nz += hs[k]->nnz + hs[k]->D;
+        }
+        BH_REQUIRE(D <= 2147483647LL, "combined dimension exceeds 2^31 - 1");
+        Stream st;
+        DevBuf<int64_t> rp(D + 1);
+        DevBuf<int32_t> ci(nz);
+        DevBuf<double> v(nz);
+        hamiltonian_multi_csr(nh, hs, order, J, U, mu, rp.p, ci.p, v.p, st);
+        BH_CUDA(cudaMemcpy(row_ptr, rp.p, (D + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost));
+        BH_CUDA(cudaMemcpy(col, ci.p, nz * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        BH_CUDA(cudaMemcpy(val, v.p, nz * sizeof(double), cudaMemcpyDeviceToHost));
+    });
+}
+
 static OpView<double> op64_of(const bh_hamiltonian* h) { return op_view<double>(h); }
 static OpView<float> op32_of(const bh_hamiltonian* h) { return op_view<float>(h); }
 

@@ -428,6 +428,34 @@ void hamiltonian_csr(const bh_hamiltonian* h, int order, double J, double U, dou
                -mu * (double)h->n, unused, nullptr, nullptr, nullptr, d_rp, d_ci, d_val, st);
 }
 
+// Moves one sector's CSR (rows and columns 0..D-1, entries from 0) to its
+// place in a block-diagonal matrix: row pointers + nnz_off, columns + row_off.
+__global__ void k_shift_csr(int64_t nrow1, int64_t* __restrict__ rp, int64_t nnz, int32_t* __restrict__ ci,
+                            int64_t row_off, int64_t nnz_off) {
+    const int64_t n = nrow1 > nnz ? nrow1 : nnz;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i < nrow1) rp[i] += nnz_off;
+        if (i < nnz) ci[i] += (int32_t)row_off;
+    }
+}
+
+void hamiltonian_multi_csr(int nh, const bh_hamiltonian* const* hs, int order, double J, double U, double mu,
+                           int64_t* d_rp, int32_t* d_ci, double* d_val, cudaStream_t st) {
+    int64_t row_off = 0, nnz_off = 0;
+    for (int k = 0; k < nh; ++k) {
+        const bh_hamiltonian* h = hs[k];
+        const int64_t nz = h->nnz + h->D;
+        hamiltonian_csr(h, order, J, U, mu, d_rp + row_off, d_ci + nnz_off, d_val + nnz_off, st);
+        const int64_t n = std::max<int64_t>(h->D + 1, nz);
+        const int64_t g = std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 8));
+        k_shift_csr<<<(unsigned)g, 256, 0, st>>>(h->D + 1, d_rp + row_off, nz, d_ci + nnz_off, row_off, nnz_off);
+        BH_CUDA(cudaGetLastError());
+        row_off += h->D;
+        nnz_off += nz;
+    }
+    BH_CUDA(cudaStreamSynchronize(st));
+}
+
 void spdm_device(const bh_hamiltonian* h, const double* d_phi_lex, double* d_rho, cudaStream_t st) {
     const bh_basis* b = h->basis;
     const int m = h->m;

@@ -155,6 +155,10 @@ int occupation_bits(int m, int n);
 // CSR of H = J T + U V - mu N with diagonal entries, rows/cols in `order`.
 void hamiltonian_csr(const bh_hamiltonian* h, int order, double J, double U, double mu,
                      int64_t* d_rp, int32_t* d_ci, double* d_val, cudaStream_t st);
+// Block-diagonal H of several sectors (in the given order), sector k's rows
+// and columns offset by the dimensions of the sectors before it.
+void hamiltonian_multi_csr(int nh, const bh_hamiltonian* const* hs, int order, double J, double U, double mu,
+                           int64_t* d_rp, int32_t* d_ci, double* d_val, cudaStream_t st);
 void spdm_device(const bh_hamiltonian* h, const double* d_phi_lex, double* d_rho,
                  cudaStream_t st);
 // out[r][0..ncols) = in[map[r]][0..ncols)  (double)

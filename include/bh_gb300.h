@@ -127,6 +127,13 @@ int bh_hamiltonian_nnz(const bh_hamiltonian* h, int64_t* nnz_offdiag);
  * sorted columns: row_ptr[D+1], col[nnz_offdiag + D], val[nnz_offdiag + D]. */
 int bh_hamiltonian_csr(const bh_hamiltonian* h, int order, double J, double U, double mu,
                        int64_t* row_ptr, int32_t* col, double* val);
+/* Replaces BH::max_bosons_hamiltonian (hamiltonian.cpp:260-288): the
+ * block-diagonal H = J T + U V - mu N of nh sectors (usually n_min..n_max of
+ * one lattice), assembled on the device, sector k's rows and columns offset
+ * by the dimensions of sectors 0..k-1, each block in `order`, one explicit
+ * diagonal entry per row: row_ptr[sum D_k + 1], col/val[sum (nnz_k + D_k)]. */
+int bh_hamiltonian_multi_csr(int nh, const bh_hamiltonian* const* hs, int order, double J, double U,
+                             double mu, int64_t* row_ptr, int32_t* col, double* val);
 /* y = H x for nvec vectors (x, y: host, row-major [D][nvec], `order`). */
 int bh_hamiltonian_apply(const bh_hamiltonian* h, int order, double J, double U, double mu,
                          int nvec, const double* x, double* y);

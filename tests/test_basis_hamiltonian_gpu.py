@@ -133,3 +133,26 @@ def test_fixed_bosons_hamiltonian_term_selection(pkg, orc):
     H = JH * 0.2 + UH * 1.0 + uH * 0.3  # analysis.cpp:311 composition
     Ho = orc.full_csr(rp, ci, tv, vd, n, 0.2, 1.0, 0.3)
     assert abs(H - Ho).max() < 1e-15
+
+
+def test_multi_sector_csr_is_the_block_diagonal_of_the_sectors(pkg):
+    # BH::max_bosons_hamiltonian (hamiltonian.cpp:260-288): sectors n_min..n_max
+    # of one lattice as one block-diagonal matrix, assembled on the device
+    import scipy.sparse as sp
+
+    m = 6
+    lists = chain_lists(m)
+    hams = [pkg.Hamiltonian(pkg.Basis(m, n), lists) for n in range(0, 5)]
+    for order in (pkg.ORDER_REFERENCE, pkg.ORDER_LEX):
+        H = pkg.multi_sector_csr(hams, 0.13, 0.9, 0.4, order=order)
+        want = sp.block_diag([h.csr(0.13, 0.9, 0.4, order=order) for h in hams], format="csr")
+        assert H.shape == want.shape
+        assert np.array_equal(H.indptr, want.indptr) and np.array_equal(H.indices, want.indices)
+        assert np.array_equal(H.data, want.data)
+    # the reference's term selection, block by block
+    for J, U, mu in ((0.1, 0.0, 0.0), (0.0, 1.0, 0.0), (0.0, 0.0, 0.7)):
+        Hm = pkg.BH.max_bosons_hamiltonian(lists, m, -1, 4, J, U, mu)
+        blocks = [pkg.BH.fixed_bosons_hamiltonian(lists, None, None, m, n, J, U, mu) for n in range(0, 5)]
+        want = sp.block_diag(blocks, format="csr")
+        assert Hm.shape == want.shape and abs(Hm - want).max() == 0.0
+        assert Hm.nnz == want.nnz

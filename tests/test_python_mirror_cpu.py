@@ -96,12 +96,41 @@ def test_max_set_basis_holds_every_state_once(pkg, orc, monkeypatch):
         assert tags[c] == pkg.BH.calculate_tag(basis, pkg.BH.PRIMES, c)
 
 
+def _fake_multi_sector(pkg, orc, monkeypatch):
+    """Device Basis / Hamiltonian / multi_sector_csr replaced by the oracle's
+    sectors (host only): the device assembly itself is a GPU test."""
+    import scipy.sparse as sp
+    from conftest import oracle_H
+
+    class FakeBasis:
+        def __init__(self, m, n):
+            self.m, self.n, self.D = m, n, pkg.BH.dimension(m, n)
+
+    class FakeHam:
+        def __init__(self, basis, lists):
+            self.basis, self.lists = basis, lists
+
+    def multi(hams, J, U, mu, order=pkg.ORDER_REFERENCE):
+        blocks = []
+        for h in hams:
+            m, n = h.basis.m, h.basis.n
+            _, _, _, rp, ci, tv, vd = oracle_H(orc, m, n, h.lists)
+            D = len(rp) - 1
+            blocks.append(sp.csr_matrix((J * tv, ci, rp), shape=(D, D)) + sp.diags(U * vd - mu * n))
+        return sp.block_diag(blocks, format="csr")
+
+    monkeypatch.setattr(pkg, "Basis", FakeBasis)
+    monkeypatch.setattr(pkg, "Hamiltonian", FakeHam)
+    monkeypatch.setattr(pkg, "multi_sector_csr", multi)
+
+
 def test_max_bosons_hamiltonian_blocks_and_clamping(pkg, orc, monkeypatch):
     from conftest import chain_lists
 
     m = 4
     lists = chain_lists(m)
     _fake_sectors(pkg, orc, monkeypatch, m, lists)
+    _fake_multi_sector(pkg, orc, monkeypatch)
     H = pkg.BH.max_bosons_hamiltonian(lists, m, -2, 3, 0.1, 0.0, 0.0)
     dims = [pkg.BH.dimension(m, k) for k in range(0, 4)]
     assert H.shape == (sum(dims), sum(dims))
