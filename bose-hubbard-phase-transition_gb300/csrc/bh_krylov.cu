@@ -613,6 +613,29 @@ k_qr_finalize(int p, int nchunks, int ncols, const double* __restrict__ gpart, i
         }
         __syncthreads();
     }
+    // final pass: the squared norms of the new directions' coefficients in the
+    // basis, sum_c T[col][c]^2 (col = (jrow - 1) p + i), summed by every thread
+    // (one serial loop over up to kmax L2 reads took most of the kernel's time)
+    __shared__ double s_pre[16];
+    const bool final_check = mode == 2 && Tm && jrow > 0;
+    if (final_check) {
+        const double* Ts = Tm + (size_t)s * Tdim * Tdim;
+        for (int i = 0; i < p; ++i) {
+            const double* trow = Ts + (size_t)((jrow - 1) * p + i) * Tdim;
+            double v = 0.0;
+            for (int c = threadIdx.x; c < jrow * p; c += QR_THREADS) v += trow[c] * trow[c];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) red[warp][i] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < p) {
+            double v = 0.0;
+            for (int w = 0; w < QR_THREADS / 32; ++w) v += red[w][threadIdx.x];
+            s_pre[threadIdx.x] = v;
+        }
+        __syncthreads();
+    }
     if (threadIdx.x != 0) return;
     double R[16][16], Ri[16][16], Rt[16][16];
     for (int a = 0; a < p; ++a)
@@ -671,14 +694,11 @@ k_qr_finalize(int p, int nchunks, int ncols, const double* __restrict__ gpart, i
     const bool final_pass = mode == 2;
     bool drop[16];
     for (int i = 0; i < p; ++i) drop[i] = R[i][i] == 0.0;
-    if (final_pass && Tm && jrow > 0) {
-        const double* Ts = Tm + (size_t)s * Tdim * Tdim;
+    if (final_check) {
         for (int i = 0; i < p; ++i) {
-            double pre = 0.0, own = 0.0;
-            const int col = (jrow - 1) * p + i;
-            for (int c = 0; c < jrow * p; ++c) pre += Ts[(size_t)col * Tdim + c] * Ts[(size_t)col * Tdim + c];
+            double own = 0.0;
             for (int k = 0; k <= i; ++k) own += Rt[k][i] * Rt[k][i];
-            if (!(fabs(Rt[i][i]) > kill_abs * sqrt(pre + own))) drop[i] = true;
+            if (!(fabs(Rt[i][i]) > kill_abs * sqrt(s_pre[i] + own))) drop[i] = true;
         }
     }
     // inverse of this pass's R on the kept directions
