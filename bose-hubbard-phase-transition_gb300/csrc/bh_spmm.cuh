@@ -189,9 +189,9 @@ __device__ __forceinline__ void sp_stv(T* __restrict__ p, const SpVec<T, VW>& o)
 // t < ncols, ncols a multiple of VW), so every gathered X row is read with
 // VW-wide vector loads and a warp's loads of one entry cover VL * VW
 // contiguous values.  Each column's sum is the same chain of fma_rn over the
-// row's entries in storage order as in k_spmm (here eight entries' rows are
-// requested before their products), and the epilogue is the same: Y equals
-// k_spmm's bit for bit.  DP > 0 (block size, DP dividing VW, one pass over the row):
+// row's entries in storage order as in k_spmm (four entries' rows requested
+// before their products), and the epilogue is the same: Y equals k_spmm's
+// bit for bit.  DP > 0 (block size, DP dividing VW, one pass over the row):
 // the lane's VW columns hold whole solves, so the partials of X_s^T Y_s need
 // no data from other lanes; FP32 sums over 16 rows, then FP64 slots in shared
 // memory, reduced per CTA into dpart[(cta DP + q) ncols + t] like k_spmm.
@@ -228,7 +228,7 @@ k_spmm_v(OpView<T> A, int ncols, int group, const double* __restrict__ prm,
             int64_t e = e0;
             // UE entries per step: their X rows are all requested before the
             // first product (the summation order per column is unchanged)
-            constexpr int UE = 8;
+            constexpr int UE = 4;  // 8 measured 6% slower at m=13 (48 registers, fewer warps)
             for (; e + UE <= e1; e += UE) {
                 int cc[UE];
                 T vv[UE];
