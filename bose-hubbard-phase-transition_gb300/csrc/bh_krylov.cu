@@ -565,6 +565,281 @@ k_updatev(int64_t D, int S, int nblk, int64_t bstride, const T* __restrict__ V,
 // The norm before orthogonalisation is sqrt(sum_c T[c][col]^2 + |Rtot_.i|^2)
 // with col = (jrow - 1) p + i, the coefficients of H v_col in the basis.
 constexpr int QR_THREADS = 128;
+// The serial part of k_qr_finalize (thread 0 of a solve's CTA): the p x p
+// Cholesky factor of G (shifted in mode 0), the accumulated factor, the
+// dropped directions, the inverse on the kept ones, and the writes.  PM is
+// the block capacity: PM <= 4 unrolls every loop so the factors stay in
+// registers; larger blocks run the same loops with the factors in local memory.
+template <int PM>
+__device__ __forceinline__ void qr_factor(int p, int s, int mode, double shift_rel, const double (*G)[16],
+                                          const double* s_pre, bool final_check, double* __restrict__ Racc,
+                                          double* __restrict__ Rinv, double* __restrict__ Tm, int Tdim, int jrow,
+                                          double kill_abs, unsigned char* __restrict__ dead,
+                                          int* __restrict__ need3) {
+    if constexpr (PM <= 4) {
+    // the p x p factors in registers: every loop below runs to the capacity
+        // PM (unrolled for PM <= 4, so the arrays are indexed by constants) and
+        // stops at p; larger blocks keep them in local memory
+        double R[PM][PM], Ri[PM][PM], Rt[PM][PM];
+#pragma unroll
+        for (int a = 0; a < PM; ++a)
+#pragma unroll
+            for (int b = 0; b < PM; ++b) {
+                R[a][b] = 0.0;
+                Ri[a][b] = 0.0;
+                Rt[a][b] = 0.0;
+            }
+        double* Ra = Racc + (size_t)s * p * p;
+        auto cholesky = [&](double shift) {
+            double dmin = INFINITY;
+#pragma unroll
+            for (int i = 0; i < PM; ++i) {
+                if (i >= p) break;
+                double d = G[i][i] + shift;
+#pragma unroll
+                for (int k = 0; k < i; ++k) d -= R[k][i] * R[k][i];
+                dmin = fmin(dmin, d);
+                R[i][i] = 0.0;
+#pragma unroll
+                for (int j = i + 1; j < PM; ++j) R[i][j] = 0.0;
+                if (!(d > 0.0)) continue;  // zero column (already dropped) stays zero
+                const double rii = sqrt(d);
+                R[i][i] = rii;
+#pragma unroll
+                for (int j = i + 1; j < PM; ++j) {
+                    if (j >= p) break;
+                    double v = 0.5 * (G[i][j] + G[j][i]);
+#pragma unroll
+                    for (int k = 0; k < i; ++k) v -= R[k][i] * R[k][j];
+                    R[i][j] = v / rii;
+                }
+            }
+            return dmin;
+        };
+        if (mode == 0) {
+            double gmax = 0.0;
+            for (int i = 0; i < p; ++i) gmax = fmax(gmax, G[i][i]);
+            // well conditioned (every pivot >= 1e-4 of the largest diagonal
+            // entry, i.e. cond(W)^2 <= 1e4): plain Cholesky, and two passes
+            // (CholQR2) orthonormalise to working precision.  Otherwise the
+            // shifted first pass, and the step needs all three.
+            bool plain = need3 != nullptr && gmax > 0.0;
+            if (plain) plain = cholesky(0.0) >= 1e-4 * gmax;
+            if (!plain) {
+                cholesky(shift_rel * gmax);
+                if (need3) atomicAdd(need3, 1);
+            }
+        } else {
+            cholesky(0.0);
+        }
+        // accumulated factor Rt = R * Racc (upper triangular products)
+#pragma unroll
+        for (int a = 0; a < PM; ++a) {
+            if (a >= p) break;
+#pragma unroll
+            for (int b = 0; b < PM; ++b) {
+                if (b >= p) break;
+                if (mode == 0 || p == 1) {
+                    Rt[a][b] = R[a][b];
+                } else {
+                    double v = 0.0;
+#pragma unroll
+                    for (int k = a; k <= b; ++k) v += R[a][k] * Ra[k * p + b];
+                    Rt[a][b] = v;
+                }
+            }
+        }
+        const bool final_pass = mode == 2;
+        bool drop[PM];
+#pragma unroll
+        for (int i = 0; i < PM; ++i) drop[i] = i < p && R[i][i] == 0.0;
+        if (final_check) {
+#pragma unroll
+            for (int i = 0; i < PM; ++i) {
+                if (i >= p) break;
+                double own = 0.0;
+#pragma unroll
+                for (int k = 0; k <= i; ++k) own += Rt[k][i] * Rt[k][i];
+                if (!(fabs(Rt[i][i]) > kill_abs * sqrt(s_pre[i] + own))) drop[i] = true;
+            }
+        }
+        // inverse of this pass's R on the kept directions
+#pragma unroll
+        for (int j = 0; j < PM; ++j) {
+            if (j >= p) break;
+            if (drop[j] && final_pass) continue;
+            if (R[j][j] == 0.0) continue;
+            Ri[j][j] = 1.0 / R[j][j];
+#pragma unroll
+            for (int i = j - 1; i >= 0; --i) {
+                if (R[i][i] == 0.0) continue;
+                double v = 0.0;
+#pragma unroll
+                for (int k = i + 1; k <= j; ++k) v += R[i][k] * Ri[k][j];
+                Ri[i][j] = -v / R[i][i];
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < PM; ++a) {
+            if (a >= p) break;
+#pragma unroll
+            for (int b = 0; b < PM; ++b) {
+                if (b >= p) break;
+                Rinv[(size_t)s * p * p + a * p + b] = Ri[a][b];
+                Ra[a * p + b] = (final_pass && drop[a]) ? 0.0 : Rt[a][b];
+            }
+        }
+        if (!final_pass) return;
+        if (Tm && jrow > 0) {
+            double* Tw = Tm + (size_t)s * Tdim * Tdim;
+#pragma unroll
+            for (int a = 0; a < PM; ++a) {
+                if (a >= p) break;
+#pragma unroll
+                for (int b = 0; b < PM; ++b) {
+                    if (b >= p) break;
+                    Tw[(size_t)((jrow - 1) * p + b) * Tdim + jrow * p + a] = drop[a] ? 0.0 : Rt[a][b];
+                }
+            }
+            if (dead)
+#pragma unroll
+                for (int a = 0; a < PM; ++a)
+                    if (a < p) dead[(size_t)s * Tdim + jrow * p + a] = drop[a] ? 1 : 0;
+        }
+    } else {
+    // the p x p factors in registers: every loop below runs to the capacity
+        // PM (unrolled for PM <= 4, so the arrays are indexed by constants) and
+        // stops at p; larger blocks keep them in local memory
+        double R[PM][PM], Ri[PM][PM], Rt[PM][PM];
+#pragma unroll 1
+        for (int a = 0; a < PM; ++a)
+#pragma unroll 1
+            for (int b = 0; b < PM; ++b) {
+                R[a][b] = 0.0;
+                Ri[a][b] = 0.0;
+                Rt[a][b] = 0.0;
+            }
+        double* Ra = Racc + (size_t)s * p * p;
+        auto cholesky = [&](double shift) {
+            double dmin = INFINITY;
+#pragma unroll 1
+            for (int i = 0; i < PM; ++i) {
+                if (i >= p) break;
+                double d = G[i][i] + shift;
+#pragma unroll 1
+                for (int k = 0; k < i; ++k) d -= R[k][i] * R[k][i];
+                dmin = fmin(dmin, d);
+                R[i][i] = 0.0;
+#pragma unroll 1
+                for (int j = i + 1; j < PM; ++j) R[i][j] = 0.0;
+                if (!(d > 0.0)) continue;  // zero column (already dropped) stays zero
+                const double rii = sqrt(d);
+                R[i][i] = rii;
+#pragma unroll 1
+                for (int j = i + 1; j < PM; ++j) {
+                    if (j >= p) break;
+                    double v = 0.5 * (G[i][j] + G[j][i]);
+#pragma unroll 1
+                    for (int k = 0; k < i; ++k) v -= R[k][i] * R[k][j];
+                    R[i][j] = v / rii;
+                }
+            }
+            return dmin;
+        };
+        if (mode == 0) {
+            double gmax = 0.0;
+            for (int i = 0; i < p; ++i) gmax = fmax(gmax, G[i][i]);
+            // well conditioned (every pivot >= 1e-4 of the largest diagonal
+            // entry, i.e. cond(W)^2 <= 1e4): plain Cholesky, and two passes
+            // (CholQR2) orthonormalise to working precision.  Otherwise the
+            // shifted first pass, and the step needs all three.
+            bool plain = need3 != nullptr && gmax > 0.0;
+            if (plain) plain = cholesky(0.0) >= 1e-4 * gmax;
+            if (!plain) {
+                cholesky(shift_rel * gmax);
+                if (need3) atomicAdd(need3, 1);
+            }
+        } else {
+            cholesky(0.0);
+        }
+        // accumulated factor Rt = R * Racc (upper triangular products)
+#pragma unroll 1
+        for (int a = 0; a < PM; ++a) {
+            if (a >= p) break;
+#pragma unroll 1
+            for (int b = 0; b < PM; ++b) {
+                if (b >= p) break;
+                if (mode == 0 || p == 1) {
+                    Rt[a][b] = R[a][b];
+                } else {
+                    double v = 0.0;
+#pragma unroll 1
+                    for (int k = a; k <= b; ++k) v += R[a][k] * Ra[k * p + b];
+                    Rt[a][b] = v;
+                }
+            }
+        }
+        const bool final_pass = mode == 2;
+        bool drop[PM];
+#pragma unroll 1
+        for (int i = 0; i < PM; ++i) drop[i] = i < p && R[i][i] == 0.0;
+        if (final_check) {
+#pragma unroll 1
+            for (int i = 0; i < PM; ++i) {
+                if (i >= p) break;
+                double own = 0.0;
+#pragma unroll 1
+                for (int k = 0; k <= i; ++k) own += Rt[k][i] * Rt[k][i];
+                if (!(fabs(Rt[i][i]) > kill_abs * sqrt(s_pre[i] + own))) drop[i] = true;
+            }
+        }
+        // inverse of this pass's R on the kept directions
+#pragma unroll 1
+        for (int j = 0; j < PM; ++j) {
+            if (j >= p) break;
+            if (drop[j] && final_pass) continue;
+            if (R[j][j] == 0.0) continue;
+            Ri[j][j] = 1.0 / R[j][j];
+#pragma unroll 1
+            for (int i = j - 1; i >= 0; --i) {
+                if (R[i][i] == 0.0) continue;
+                double v = 0.0;
+#pragma unroll 1
+                for (int k = i + 1; k <= j; ++k) v += R[i][k] * Ri[k][j];
+                Ri[i][j] = -v / R[i][i];
+            }
+        }
+#pragma unroll 1
+        for (int a = 0; a < PM; ++a) {
+            if (a >= p) break;
+#pragma unroll 1
+            for (int b = 0; b < PM; ++b) {
+                if (b >= p) break;
+                Rinv[(size_t)s * p * p + a * p + b] = Ri[a][b];
+                Ra[a * p + b] = (final_pass && drop[a]) ? 0.0 : Rt[a][b];
+            }
+        }
+        if (!final_pass) return;
+        if (Tm && jrow > 0) {
+            double* Tw = Tm + (size_t)s * Tdim * Tdim;
+#pragma unroll 1
+            for (int a = 0; a < PM; ++a) {
+                if (a >= p) break;
+#pragma unroll 1
+                for (int b = 0; b < PM; ++b) {
+                    if (b >= p) break;
+                    Tw[(size_t)((jrow - 1) * p + b) * Tdim + jrow * p + a] = drop[a] ? 0.0 : Rt[a][b];
+                }
+            }
+            if (dead)
+#pragma unroll 1
+                for (int a = 0; a < PM; ++a)
+                    if (a < p) dead[(size_t)s * Tdim + jrow * p + a] = drop[a] ? 1 : 0;
+        }
+    }
+}
+
+template <int PM>
 __global__ void __launch_bounds__(QR_THREADS)
 k_qr_finalize(int p, int nchunks, int ncols, const double* __restrict__ gpart, int mode,
               double shift_rel, double* __restrict__ Racc, double* __restrict__ Rinv,
@@ -637,95 +912,7 @@ k_qr_finalize(int p, int nchunks, int ncols, const double* __restrict__ gpart, i
         __syncthreads();
     }
     if (threadIdx.x != 0) return;
-    double R[16][16], Ri[16][16], Rt[16][16];
-    for (int a = 0; a < p; ++a)
-        for (int b = 0; b < p; ++b) {
-            R[a][b] = 0.0;
-            Ri[a][b] = 0.0;
-            Rt[a][b] = 0.0;
-        }
-    double* Ra = Racc + (size_t)s * p * p;
-    auto cholesky = [&](double shift) {
-        double dmin = INFINITY;
-        for (int i = 0; i < p; ++i) {
-            double d = G[i][i] + shift;
-            for (int k = 0; k < i; ++k) d -= R[k][i] * R[k][i];
-            dmin = fmin(dmin, d);
-            R[i][i] = 0.0;
-            for (int j = i + 1; j < p; ++j) R[i][j] = 0.0;
-            if (!(d > 0.0)) continue;  // zero column (already dropped) stays zero
-            const double rii = sqrt(d);
-            R[i][i] = rii;
-            for (int j = i + 1; j < p; ++j) {
-                double v = 0.5 * (G[i][j] + G[j][i]);
-                for (int k = 0; k < i; ++k) v -= R[k][i] * R[k][j];
-                R[i][j] = v / rii;
-            }
-        }
-        return dmin;
-    };
-    if (mode == 0) {
-        double gmax = 0.0;
-        for (int i = 0; i < p; ++i) gmax = fmax(gmax, G[i][i]);
-        // well conditioned (every pivot >= 1e-4 of the largest diagonal
-        // entry, i.e. cond(W)^2 <= 1e4): plain Cholesky, and two passes
-        // (CholQR2) orthonormalise to working precision.  Otherwise the
-        // shifted first pass, and the step needs all three.
-        bool plain = need3 != nullptr && gmax > 0.0;
-        if (plain) plain = cholesky(0.0) >= 1e-4 * gmax;
-        if (!plain) {
-            cholesky(shift_rel * gmax);
-            if (need3) atomicAdd(need3, 1);
-        }
-    } else {
-        cholesky(0.0);
-    }
-    // accumulated factor Rt = R * Racc (upper triangular products)
-    for (int a = 0; a < p; ++a)
-        for (int b = 0; b < p; ++b) {
-            if (mode == 0 || p == 1) {
-                Rt[a][b] = R[a][b];
-            } else {
-                double v = 0.0;
-                for (int k = a; k <= b; ++k) v += R[a][k] * Ra[k * p + b];
-                Rt[a][b] = v;
-            }
-        }
-    const bool final_pass = mode == 2;
-    bool drop[16];
-    for (int i = 0; i < p; ++i) drop[i] = R[i][i] == 0.0;
-    if (final_check) {
-        for (int i = 0; i < p; ++i) {
-            double own = 0.0;
-            for (int k = 0; k <= i; ++k) own += Rt[k][i] * Rt[k][i];
-            if (!(fabs(Rt[i][i]) > kill_abs * sqrt(s_pre[i] + own))) drop[i] = true;
-        }
-    }
-    // inverse of this pass's R on the kept directions
-    for (int j = 0; j < p; ++j) {
-        if (drop[j] && final_pass) continue;
-        if (R[j][j] == 0.0) continue;
-        Ri[j][j] = 1.0 / R[j][j];
-        for (int i = j - 1; i >= 0; --i) {
-            if (R[i][i] == 0.0) continue;
-            double v = 0.0;
-            for (int k = i + 1; k <= j; ++k) v += R[i][k] * Ri[k][j];
-            Ri[i][j] = -v / R[i][i];
-        }
-    }
-    for (int a = 0; a < p; ++a)
-        for (int b = 0; b < p; ++b) Rinv[(size_t)s * p * p + a * p + b] = Ri[a][b];
-    for (int a = 0; a < p; ++a)
-        for (int b = 0; b < p; ++b) Ra[a * p + b] = (final_pass && drop[a]) ? 0.0 : Rt[a][b];
-    if (!final_pass) return;
-    if (Tm && jrow > 0) {
-        double* Tw = Tm + (size_t)s * Tdim * Tdim;
-        for (int a = 0; a < p; ++a)
-            for (int b = 0; b < p; ++b)
-                Tw[(size_t)((jrow - 1) * p + b) * Tdim + jrow * p + a] = drop[a] ? 0.0 : Rt[a][b];
-        if (dead)
-            for (int a = 0; a < p; ++a) dead[(size_t)s * Tdim + jrow * p + a] = drop[a] ? 1 : 0;
-    }
+    qr_factor<PM>(p, s, mode, shift_rel, G, s_pre, final_check, Racc, Rinv, Tm, Tdim, jrow, kill_abs, dead, need3);
 }
 
 // V[r][s p + q'] = sum_{q <= q'} W[r][s p + q] Rinv_s[q][q']
@@ -1492,8 +1679,15 @@ struct Launcher {
             double* Racc, double* Rinv, double* Tm, int Tdim, int jrow, double kill_abs,
             unsigned char* dead, int* need3 = nullptr) const {
         profile_begin(st);
-        k_qr_finalize<<<S, QR_THREADS, 0, st>>>(p, gu.nchunks, gu.ncols, gpart, mode, shift_rel, Racc,
-                                                Rinv, Tm, Tdim, jrow, kill_abs, dead, need3);
+        auto go = [&](auto kern) {
+            kern<<<S, QR_THREADS, 0, st>>>(p, gu.nchunks, gu.ncols, gpart, mode, shift_rel, Racc, Rinv, Tm, Tdim,
+                                          jrow, kill_abs, dead, need3);
+        };
+        if (p <= 1) go(k_qr_finalize<1>);
+        else if (p <= 2) go(k_qr_finalize<2>);
+        else if (p <= 4) go(k_qr_finalize<4>);
+        else if (p <= 8) go(k_qr_finalize<8>);
+        else go(k_qr_finalize<16>);
         done("k_qr_finalize", (double)gu.nchunks * p * gu.ncols * 8.0);
     }
     template <int P>
