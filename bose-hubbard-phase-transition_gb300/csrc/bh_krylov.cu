@@ -572,7 +572,8 @@ constexpr int QR_THREADS = 128;
 // registers; larger blocks run the same loops with the factors in local memory.
 template <int PM>
 __device__ __forceinline__ void qr_factor(int p, int s, int mode, double shift_rel, const double (*G)[16],
-                                          const double* s_pre, bool final_check, double* __restrict__ Racc,
+                                          const double* s_pre, const double* sRa, bool final_check,
+                                          double* __restrict__ Racc,
                                           double* __restrict__ Rinv, double* __restrict__ Tm, int Tdim, int jrow,
                                           double kill_abs, unsigned char* __restrict__ dead,
                                           int* __restrict__ need3) {
@@ -644,7 +645,7 @@ __device__ __forceinline__ void qr_factor(int p, int s, int mode, double shift_r
                 } else {
                     double v = 0.0;
 #pragma unroll
-                    for (int k = a; k <= b; ++k) v += R[a][k] * Ra[k * p + b];
+                    for (int k = a; k <= b; ++k) v += R[a][k] * sRa[k * p + b];
                     Rt[a][b] = v;
                 }
             }
@@ -774,7 +775,7 @@ __device__ __forceinline__ void qr_factor(int p, int s, int mode, double shift_r
                 } else {
                     double v = 0.0;
 #pragma unroll 1
-                    for (int k = a; k <= b; ++k) v += R[a][k] * Ra[k * p + b];
+                    for (int k = a; k <= b; ++k) v += R[a][k] * sRa[k * p + b];
                     Rt[a][b] = v;
                 }
             }
@@ -845,74 +846,96 @@ k_qr_finalize(int p, int nchunks, int ncols, const double* __restrict__ gpart, i
               double shift_rel, double* __restrict__ Racc, double* __restrict__ Rinv,
               double* __restrict__ Tm, int Tdim, int jrow, double kill_abs,
               unsigned char* __restrict__ dead, int* __restrict__ need3) {
+    // entries of G reduced per pass: the whole p x p block for p <= 4
+    constexpr int NE = PM * PM < 16 ? PM * PM : 16;
     __shared__ double G[16][16];
     __shared__ double red[QR_THREADS / 32][16];
+    __shared__ double red_pre[QR_THREADS / 32][PM];
+    __shared__ double s_pre[16];
+    __shared__ double s_ra[PM * PM];
     const int s = blockIdx.x;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // final pass of a step whose blocks were all well conditioned: the middle
-    // Gram pass was skipped and the block is already orthonormal (G = I)
-    const bool skipped = mode == 2 && need3 && *need3 == 0;
+    // The kernel is a chain of dependent L2 round trips for one CTA per solve,
+    // so every global load is issued up front: the skip flag, the chunk
+    // partials of G, the coefficient rows of the final check and the
+    // accumulated factor all go out before the first reduction waits on them.
+    //
+    // Final pass of a step whose blocks were all well conditioned: the middle
+    // Gram pass was skipped and the block is already orthonormal (G = I).  The
+    // partials are read either way (a live buffer; the values are then unused).
+    const int n3 = (mode == 2 && need3) ? *need3 : 1;
+    // accumulated factor of the earlier passes, read by the serial part
+    if (mode != 0 && p > 1)
+        for (int e = threadIdx.x; e < p * p; e += QR_THREADS) s_ra[e] = Racc[(size_t)s * p * p + e];
+    // final pass: the squared norms of the new directions' coefficients in the
+    // basis, sum_c T[col][c]^2 (col = (jrow - 1) p + i), summed by every thread
+    const bool final_check = mode == 2 && Tm && jrow > 0;
+    double pre[PM];
+#pragma unroll
+    for (int i = 0; i < PM; ++i) pre[i] = 0.0;
+    if (final_check) {
+        const double* Ts = Tm + (size_t)s * Tdim * Tdim + (size_t)(jrow - 1) * p * Tdim;
+        for (int c = threadIdx.x; c < jrow * p; c += QR_THREADS)
+#pragma unroll
+            for (int i = 0; i < PM; ++i)
+                if (i < p) {
+                    const double t = Ts[(size_t)i * Tdim + c];
+                    pre[i] += t * t;
+                }
+    }
     // G = sum of the chunk partials: every thread sums the chunks
     // tid, tid + QR_THREADS, ... of each entry (independent loads in flight),
     // then a fixed-order reduction over the lanes and the warps
-    for (int e0 = 0; e0 < p * p; e0 += 16) {
-        const int ne = min(16, p * p - e0);
-        double acc[16];
+    for (int e0 = 0; e0 < p * p; e0 += NE) {
+        const int ne = min(NE, p * p - e0);
+        double acc[NE];
+        int off[NE];
 #pragma unroll
-        for (int k = 0; k < 16; ++k) acc[k] = 0.0;
-        if (!skipped) {
-            for (int ch = threadIdx.x; ch < nchunks; ch += QR_THREADS) {
-                const double* gp = gpart + (size_t)ch * p * ncols;
+        for (int k = 0; k < NE; ++k) {
+            acc[k] = 0.0;
+            const int e = min(e0 + k, p * p - 1), a = e / p, b = e % p;
+            off[k] = a * ncols + s * p + b;
+        }
+#pragma unroll 4
+        for (int ch = threadIdx.x; ch < nchunks; ch += QR_THREADS) {
+            const double* gp = gpart + (size_t)ch * p * ncols;
 #pragma unroll
-                for (int k = 0; k < 16; ++k) {
-                    if (k < ne) {
-                        const int e = e0 + k, a = e / p, b = e % p;
-                        acc[k] += gp[(size_t)a * ncols + s * p + b];
-                    }
-                }
-            }
+            for (int k = 0; k < NE; ++k)
+                if (k < ne) acc[k] += gp[off[k]];
         }
 #pragma unroll
-        for (int k = 0; k < 16; ++k) {
+        for (int k = 0; k < NE; ++k) {
             double v = acc[k];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
             if (lane == 0) red[warp][k] = v;
+        }
+        if (e0 == 0 && final_check) {
+#pragma unroll
+            for (int i = 0; i < PM; ++i) {
+                double v = pre[i];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                if (lane == 0) red_pre[warp][i] = v;
+            }
         }
         __syncthreads();
         if (threadIdx.x < ne) {
             const int e = e0 + threadIdx.x, a = e / p, b = e % p;
             double v = 0.0;
             for (int w = 0; w < QR_THREADS / 32; ++w) v += red[w][threadIdx.x];
-            G[a][b] = skipped ? (a == b ? 1.0 : 0.0) : v;
+            G[a][b] = n3 == 0 ? (a == b ? 1.0 : 0.0) : v;
         }
-        __syncthreads();
-    }
-    // final pass: the squared norms of the new directions' coefficients in the
-    // basis, sum_c T[col][c]^2 (col = (jrow - 1) p + i), summed by every thread
-    // (one serial loop over up to kmax L2 reads took most of the kernel's time)
-    __shared__ double s_pre[16];
-    const bool final_check = mode == 2 && Tm && jrow > 0;
-    if (final_check) {
-        const double* Ts = Tm + (size_t)s * Tdim * Tdim;
-        for (int i = 0; i < p; ++i) {
-            const double* trow = Ts + (size_t)((jrow - 1) * p + i) * Tdim;
+        if (e0 == 0 && final_check && threadIdx.x >= 32 && threadIdx.x < 32 + p) {
+            const int i = threadIdx.x - 32;
             double v = 0.0;
-            for (int c = threadIdx.x; c < jrow * p; c += QR_THREADS) v += trow[c] * trow[c];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane == 0) red[warp][i] = v;
-        }
-        __syncthreads();
-        if (threadIdx.x < p) {
-            double v = 0.0;
-            for (int w = 0; w < QR_THREADS / 32; ++w) v += red[w][threadIdx.x];
-            s_pre[threadIdx.x] = v;
+            for (int w = 0; w < QR_THREADS / 32; ++w) v += red_pre[w][i];
+            s_pre[i] = v;
         }
         __syncthreads();
     }
     if (threadIdx.x != 0) return;
-    qr_factor<PM>(p, s, mode, shift_rel, G, s_pre, final_check, Racc, Rinv, Tm, Tdim, jrow, kill_abs, dead, need3);
+    qr_factor<PM>(p, s, mode, shift_rel, G, s_pre, s_ra, final_check, Racc, Rinv, Tm, Tdim, jrow, kill_abs, dead, need3);
 }
 
 // V[r][s p + q'] = sum_{q <= q'} W[r][s p + q] Rinv_s[q][q']
