@@ -425,6 +425,18 @@ def run_ours(args):
         out["kernel_gbs"] = {k: round(v["bytes"] / (v["ms"] * 1e6), 1)
                              for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"]) if v["ms"] > 0}
 
+        # the sparse product against the bytes it must gather (every entry
+        # pulls a whole row of X), on the largest sector solved alone, whose
+        # D and entry count fix the bytes of each launch
+        pkg.profile_reset()
+        pkg.profile_enable(True)
+        hams[-1].eigsh_batch(js, U, 0.0, nev=NEV, precision=pkg.PREC_MIXED)
+        pkg.profile_enable(False)
+        gather = _spmm_gather(pkg.profile_read(), hams[-1], False)
+        if gather:
+            gather["sector"] = f"n={SECTORS[-1]} alone (D={hams[-1].D}), {len(js)} J"
+        out["spmm_gather"] = gather
+
         # launch shapes the autotuner chose for the unfused products of the
         # bench's sectors (timed during the first warm-up step, while the five
         # sectors run concurrently)

@@ -1566,6 +1566,7 @@ struct Launcher {
     int64_t* launches;
     int* tc_status = nullptr;  // error flag of the tensor-core rotation (device)
 
+    void profile_begin_() const { profile_begin(st); }
     void done(const char* name, double bytes) const {
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) throw Error(BH_ERR_CUDA, std::string("launch of ") + name + ": " + cudaGetErrorString(e));
@@ -2448,16 +2449,18 @@ SolveResult block_lanczos(const OpView<double>& op64, const OpView<float>& op32,
             const Geo gg = make_geo(D, ns * K);
             const int64_t off = (int64_t)s0 * K;
             const int64_t zoff = off * K;
+            // operands read once (Y1, X1 and the second pair when present), result written once
+            const int nin = (Y1 ? 1 : 0) + (X1 ? 1 : 0) + (Y2 ? 1 : 0) + (X2 ? 1 : 0);
+            L.profile_begin_();
             k_ritz_mix<<<gg.nchunks, gg.NT, norms ? gg.NT * sizeof(double) : 0, st>>>(
                 D, ns * K, nc2, K, Y1 + off, X1 ? X1 + off : nullptr, Z1 + zoff, Y2 ? Y2 + off : nullptr,
                 X2 ? X2 + off : nullptr, Z2 ? Z2 + zoff : nullptr, theta ? theta + off : nullptr,
                 out ? out + off : nullptr, gg.rows_per_chunk, norms ? rpart.p : nullptr);
-            BH_CUDA(cudaGetLastError());
-            ++res.launches;
+            L.done("k_ritz_mix", (double)(nin + (out ? 1 : 0)) * D * ns * K * sizeof(double));
             if (norms) {
+                L.profile_begin_();
                 k_sum_cols<<<(ns * K + 255) / 256, 256, 0, st>>>(gg.nchunks, ns * K, rpart.p, norms + off);
-                BH_CUDA(cudaGetLastError());
-                ++res.launches;
+                L.done("k_sum_cols", (double)gg.nchunks * ns * K * sizeof(double));
             }
         }
     };
