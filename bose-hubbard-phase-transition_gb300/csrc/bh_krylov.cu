@@ -1485,6 +1485,18 @@ static bool tc_rotation_on() {
     return v == 1;
 }
 
+// BH_TMA_ROTATE=1: the restart rotation of a batch whose solves all continue
+// streamed by TMA into warp-specialised TF32 tensor-core products
+// (bh_rotate_tma.cu) instead of the SIMT kernel
+static bool tma_rotation_on() {
+    static int v = -1;
+    if (v < 0) {
+        const char* e = std::getenv("BH_TMA_ROTATE");
+        v = (e && *e == '1') ? 1 : 0;
+    }
+    return v == 1;
+}
+
 static bool debug_ortho() {
     static int v = -1;
     if (v < 0) {
@@ -1741,11 +1753,21 @@ struct Launcher {
         done("k_normalize", 2.0 * op.D * ncols * sizeof(T));
     }
     // rotation of Sproc solves (see k_rotate); Yg is Sproc x kc x nout
+    // contiguous: the processed solves are 0 .. Sproc - 1 in and out (no solve
+    // retired at this restart)
     void rotate(int Sproc, int ld_in, int p, int kc, int nout, int64_t bstride, const T* V,
                 const T* Yg, const int* in_idx, const int* out_idx, T* Vout, int64_t ostride,
-                int ld_out, int single) const {
+                int ld_out, int single, bool contiguous = false) const {
         if (Sproc <= 0) return;
         if constexpr (std::is_same<T, float>::value) {
+            if (contiguous && !single && tma_rotation_on()) {
+                profile_begin(st);
+                if (rotate_tma(op.D, Sproc, ld_in, p, kc, nout, bstride, V, Yg, Vout, ostride, ld_out, tc_status,
+                               st)) {
+                    done("k_rotate_tma", (double)op.D * Sproc * p * ((double)kc / p + (double)nout / p) * sizeof(T));
+                    return;
+                }
+            }
             // FP32 basis: the tensor-core rotation (bh_rotate_tc.cu) where its
             // shapes allow, else the SIMT kernel below
             if (tc_rotation_on()) {
@@ -2287,7 +2309,8 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
         BH_CUDA(cudaMemcpyAsync(Yd.p, Yt.data(), Yt.size() * sizeof(T), cudaMemcpyHostToDevice, st));
         BH_CUDA(cudaMemcpyAsync(d_in.p, in.data(), nc * sizeof(int), cudaMemcpyHostToDevice, st));
         BH_CUDA(cudaMemcpyAsync(d_out.p, out.data(), nc * sizeof(int), cudaMemcpyHostToDevice, st));
-        L.rotate(nc, ncols, p, kmax, nkeep, bstride, Va.p, Yd.p, d_in.p, d_out.p, Vb.p, bstride2, ncols2, 0);
+        L.rotate(nc, ncols, p, kmax, nkeep, bstride, Va.p, Yd.p, d_in.p, d_out.p, Vb.p, bstride2, ncols2, 0,
+                 nc == S);
         L.gather_block(nc, p, ncols, ncols2, d_in.p, Va.p + (int64_t)nb * bstride,
                        Vb.p + (int64_t)(nkeep / p) * bstride2);
         std::swap(Va.p, Vb.p);  // equal sizes: ownership stays balanced

@@ -270,6 +270,12 @@ void apply_operator_raw(const OpView<double>& op, int ncols, int group, const do
 bool rotate_tc(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t bstride, const float* V,
                const float* Yg, const int* in_idx, const int* out_idx, float* Vout, int64_t ostride,
                int ld_out, int single, int* d_status, cudaStream_t st);
+// The same rotation streamed by TMA with warp-specialised TF32 tensor-core
+// products (bh_rotate_tma.cu), for a batch whose solves all continue (input
+// and output solve indices the identity, not the single-array layout).
+// Returns false, launching nothing, when the shapes or alignments do not fit.
+bool rotate_tma(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t bstride, const float* V,
+                const float* Yg, float* Vout, int64_t ostride, int ld_out, int* d_status, cudaStream_t st);
 
 SolveResult block_lanczos(const OpView<double>& op64, const OpView<float>& op32,
                           const SolveRequest& rq, cudaStream_t st);

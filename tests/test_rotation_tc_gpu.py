@@ -1,7 +1,9 @@
 """GPU: the thick-restart rotation of the FP32 Krylov basis on the tensor
-cores (tcgen05.mma kind::tf32 with three-piece TF32 splits, bh_rotate_tc.cu,
-BH_TC_ROTATE=1) against the SIMT rotation (the default, BH_TC_ROTATE=0), each in
-a child process because the switch is read once per process.  Both solves must give the FP64 path's
+cores -- tcgen05.mma kind::tf32 with three-piece TF32 splits (bh_rotate_tc.cu,
+BH_TC_ROTATE=1), and the TMA-streamed, warp-specialised form with two-piece
+splits (bh_rotate_tma.cu, BH_TMA_ROTATE=1, for the restarts at which every
+solve continues) -- against the SIMT rotation (the default), each in a child
+process because the switches are read once per process.  Every solve must give the FP64 path's
 eigenvalues within 1e-8 (pure relative), for block sizes 1, 2 and 4 (the
 tensor-core kernel's three layouts of a basis row).  Block 1 runs on the open
 chain: the periodic chain's degenerate pairs need a block of 2 (one Krylov
@@ -48,8 +50,13 @@ print(json.dumps(out))
 """
 
 
-def _solve_all(env_tc: str):
-    env = dict(os.environ, BH_TC_ROTATE=env_tc)
+MODES = {"tensor cores": {"BH_TC_ROTATE": "1", "BH_TMA_ROTATE": "0"},
+         "TMA + tensor cores": {"BH_TC_ROTATE": "0", "BH_TMA_ROTATE": "1"},
+         "SIMT": {"BH_TC_ROTATE": "0", "BH_TMA_ROTATE": "0"}}
+
+
+def _solve_all(mode: str):
+    env = dict(os.environ, **MODES[mode])
     code = CHILD.format(root=ROOT, cases=CASES)
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=900)
     assert r.returncode == 0, r.stderr[-3000:]
@@ -57,9 +64,8 @@ def _solve_all(env_tc: str):
 
 
 def test_tensor_core_rotation_matches_simt_and_fp64(pkg):
-    tc = _solve_all("1")
-    simt = _solve_all("0")
-    for (m, n, lat, block, nj, nev), a, b in zip(CASES, tc, simt):
+    res = {mode: _solve_all(mode) for mode in MODES}
+    for k, (m, n, lat, block, nj, nev) in enumerate(CASES):
         nb = pkg.Neighbours(m)
         if lat == "square":
             nb.square_neighbours()
@@ -68,8 +74,8 @@ def test_tensor_core_rotation_matches_simt_and_fp64(pkg):
         h = pkg.Hamiltonian(pkg.Basis(m, n), nb.getNeighbours())
         Js = 0.3 * (np.arange(nj) + 1) / nj
         ev64, _, nc64, _ = h.eigsh_batch(Js, 1.0, 0.0, nev=nev, block=block, precision=pkg.PREC_FP64)
-        ea, eb = np.array(a["ev"]), np.array(b["ev"])
-        assert min(a["nc"]) == nev and min(b["nc"]) == nev
-        for name, e in (("tensor cores", ea), ("SIMT", eb)):
-            rel = np.abs(e - ev64) / np.abs(ev64)
-            assert rel.max() < 1e-8, (name, m, n, lat, block, rel.max())
+        for mode in MODES:
+            r = res[mode][k]
+            assert min(r["nc"]) == nev, (mode, m, n, lat, block)
+            rel = np.abs(np.array(r["ev"]) - ev64) / np.abs(ev64)
+            assert rel.max() < 1e-8, (mode, m, n, lat, block, rel.max())
