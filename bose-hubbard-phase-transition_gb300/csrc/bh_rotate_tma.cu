@@ -124,17 +124,17 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
                  : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-    uint32_t r[16];
+// 16 consecutive accumulator columns of this warp's 32 lanes; the caller waits
+// (tmem_wait) before using them, so several loads share one wait
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
+
+__device__ __forceinline__ void tmem_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 }  // namespace
 
@@ -311,10 +311,11 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
             const int64_t r = r0 + t * RT_M + row;
             const bool live = r < r1;
             for (int c0 = 0; c0 < npad; c0 += 16) {
-                float v[G][16];
+                uint32_t v[G][16];
 #pragma unroll
                 for (int g = 0; g < G; ++g)
                     tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((acc * G + g) * npad + c0), v[g]);
+                tmem_wait();
                 if (!live) continue;
                 // outputs c0 .. c0 + 15: blocks c0 / P ..; one block of a row
                 // holds the G solves' P outputs, 8 contiguous floats
@@ -326,13 +327,15 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
 #pragma unroll
                     for (int g = 0; g < G; ++g)
 #pragma unroll
-                        for (int q = 0; q < P; ++q) w[g * P + q] = (g < nsg) ? v[g][bb * P + q] : 0.f;
+                        for (int q = 0; q < P; ++q) w[g * P + q] = __uint_as_float(v[g][bb * P + q]);
                     float* dst = Vout + (int64_t)(i0 / P) * ostride + r * ld_out + (int64_t)sg0 * P;
                     if (nsg == G) {
                         reinterpret_cast<float4*>(dst)[0] = make_float4(w[0], w[1], w[2], w[3]);
                         reinterpret_cast<float4*>(dst)[1] = make_float4(w[4], w[5], w[6], w[7]);
                     } else {
-                        for (int e = 0; e < nsg * P; ++e) dst[e] = w[e];
+#pragma unroll
+                        for (int e = 0; e < 8; ++e)
+                            if (e < nsg * P) dst[e] = w[e];
                     }
                 }
             }
