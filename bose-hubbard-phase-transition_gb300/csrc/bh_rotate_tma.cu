@@ -9,15 +9,16 @@
 // 128-row tiles.  Warp roles:
 //   * warp 0, one lane: per K-step (8 basis vectors = 8/p blocks) one TMA box
 //     {G p columns, 128 rows, 8/p blocks} into a ring of raw stages;
-//   * warps 2..5 (thread = row): split each FP32 value x into two TF32 pieces
-//     x_hi = tf32(x), x_lo = tf32(x - x_hi) and store both in the UMMA K-major
-//     layout (core matrices of 8 rows x 16 bytes);
+//   * warps 2..9 (thread = row and half of the CTA's solves): split each FP32
+//     value x into two TF32 pieces, x_hi = x with its 13 low mantissa bits
+//     cleared (exact) and x_lo = tf32(x - x_hi), and store both in the UMMA
+//     K-major layout (core matrices of 8 rows x 16 bytes);
 //   * warp 1, one lane: per K-step and solve the three products
 //     x_hi y_hi + x_hi y_lo + x_lo y_hi as tcgen05.mma kind::tf32
 //     M=128 x N=npad x K=8 into the solve's FP32 accumulator in tensor memory
 //     (two accumulator sets, so a tile's products overlap the previous tile's
 //     read-back);
-//   * warps 6..9 (thread = row): read a finished tile's accumulators with
+//   * warps 10..13 (thread = row): read a finished tile's accumulators with
 //     tcgen05.ld and write the G solves' outputs of one block of a row as two
 //     16-byte stores.
 // The dropped product x_lo y_lo and the truncation of the pieces leave a
@@ -38,7 +39,7 @@ namespace {
 
 constexpr int RT_M = 128;                 // rows per tile = tensor-memory lanes
 constexpr int RT_KS = 8;                  // TF32 values per MMA K-step
-constexpr int RT_THREADS = 320;           // 10 warps
+constexpr int RT_THREADS = 448;           // 14 warps
 constexpr unsigned RT_SPIN = 1u << 24;    // polls of an mbarrier before giving up
 constexpr int RT_HEADER = 1024;           // bytes before the tiles (barriers, flags)
 constexpr int RT_MAX_RAW = 4, RT_MAX_A = 2;
@@ -77,6 +78,13 @@ __device__ __forceinline__ float tf32_rna(float x) {
     uint32_t r;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
     return __uint_as_float(r);
+}
+
+// x = hi + lo with hi a TF32 value (x truncated to 10 mantissa bits, exact)
+// and lo the rest rounded to TF32: |x - hi - lo| <= 2^-21 |x|
+__device__ __forceinline__ void split2(float x, float& hi, float& lo) {
+    hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+    lo = tf32_rna(x - hi);
 }
 
 // waits for the completion of the phase with this parity; false on timeout
@@ -134,6 +142,12 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
         : "r"(taddr));
 }
 
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
+
 __device__ __forceinline__ void tmem_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 }  // namespace
@@ -165,10 +179,10 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
     if (tid == 0) {
         for (int i = 0; i < NR; ++i) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar(B_RAW_FULL + i)));
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(bar(B_RAW_EMPTY + i)));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 8;" ::"r"(bar(B_RAW_EMPTY + i)));
         }
         for (int i = 0; i < NA; ++i) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(bar(B_A_FULL + i)));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 8;" ::"r"(bar(B_A_FULL + i)));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar(B_A_EMPTY + i)));
         }
         for (int i = 0; i < 2; ++i) {
@@ -193,7 +207,8 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
         const int g = e / (kcp * npad), rem = e - g * (kcp * npad);
         const int c = rem / npad, o = rem - c * npad;
         const float y = (g < nsg && c < kc && o < nout) ? Yg[((size_t)(sg0 + g) * kc + c) * nout + o] : 0.f;
-        const float y0 = tf32_rna(y), y1 = tf32_rna(y - y0);
+        float y0, y1;
+        split2(y, y0, y1);
         unsigned char* base = sB + ((size_t)(g * 2) * nks + c / RT_KS) * btile + tile_off(o, c & 7);
         *reinterpret_cast<float*>(base) = y0;
         *reinterpret_cast<float*>(base + (size_t)nks * btile) = y1;
@@ -257,22 +272,23 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
                 *reinterpret_cast<volatile int*>(s_rt + OFF_NMMA) = (int)(s + 1);
             }
         }
-    } else if (warp < 6) {
-        // ---- converters: thread = row of the tile ----
-        const int row = tid - 64;  // 0..127
+    } else if (warp < 10) {
+        // ---- converters: thread = row of the tile, warps 2..5 and 6..9 take
+        // the first and second half of the CTA's solves ----
+        constexpr int GH = G / 2;  // solves per converter thread
         const int cw = warp - 2;
+        const int row = (cw & 3) * 32 + lane;
+        const int half = cw >> 2;
         for (int64_t s = 0; s < nstep; ++s) {
             const int rs = (int)(s % NR);
             if (!wait_full(bar(B_RAW_FULL + rs), s / NR, err)) break;
-            // this row's G P values of each of the KB blocks: 32 bytes per block
-            float x[KB][8];
-            const unsigned char* raw = sRaw + (size_t)rs * RAW + (size_t)row * 32;
+            // this row's GH P values of each of the KB blocks: 16 bytes per block
+            float x[KB][4];
+            const unsigned char* raw = sRaw + (size_t)rs * RAW + (size_t)row * 32 + half * 16;
 #pragma unroll
             for (int b = 0; b < KB; ++b) {
                 const float4 u = *reinterpret_cast<const float4*>(raw + (size_t)b * RT_M * 32);
-                const float4 w = *reinterpret_cast<const float4*>(raw + (size_t)b * RT_M * 32 + 16);
                 x[b][0] = u.x; x[b][1] = u.y; x[b][2] = u.z; x[b][3] = u.w;
-                x[b][4] = w.x; x[b][5] = w.y; x[b][6] = w.z; x[b][7] = w.w;
             }
             __syncwarp();
             if (lane == 0) bar_arrive(bar(B_RAW_EMPTY + rs));
@@ -281,14 +297,12 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
             unsigned char* aS = sA + (size_t)as * G * 2 * ATILE;
             const uint32_t o = tile_off(row, 0);
 #pragma unroll
-            for (int g = 0; g < G; ++g) {
+            for (int gg = 0; gg < GH; ++gg) {
+                const int g = half * GH + gg;
                 float hi[8], lo[8];
 #pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    const float v = x[k / P][g * P + k % P];  // K index k = block (k / P), value k % P
-                    hi[k] = tf32_rna(v);
-                    lo[k] = tf32_rna(v - hi[k]);
-                }
+                for (int k = 0; k < 8; ++k)  // K index k = block (k / P), value k % P
+                    split2(x[k / P][gg * P + k % P], hi[k], lo[k]);
                 unsigned char* ah = aS + (size_t)g * 2 * ATILE + o;
                 *reinterpret_cast<float4*>(ah) = make_float4(hi[0], hi[1], hi[2], hi[3]);
                 *reinterpret_cast<float4*>(ah + 128) = make_float4(hi[4], hi[5], hi[6], hi[7]);
@@ -298,10 +312,9 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncwarp();
             if (lane == 0) bar_arrive(bar(B_A_FULL + as));
-            (void)cw;
         }
     } else {
-        // ---- read-back: warp 6 + q reads tensor-memory lanes 32 ((6 + q) % 4) .. + 31 ----
+        // ---- read-back: warp 10 + q reads tensor-memory lanes 32 ((10 + q) % 4) .. + 31 ----
         const int quarter = warp & 3;
         const int row = quarter * 32 + lane;
         for (int64_t t = 0; t < ntile; ++t) {
@@ -310,17 +323,23 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const int64_t r = r0 + t * RT_M + row;
             const bool live = r < r1;
-            for (int c0 = 0; c0 < npad; c0 += 16) {
-                uint32_t v[G][16];
+            // CW accumulator columns of every solve per chunk (8 when 8 solves
+            // share the CTA, so that the chunk stays in registers)
+            constexpr int CW = G > 4 ? 8 : 16;
+            for (int c0 = 0; c0 < npad; c0 += CW) {
+                uint32_t v[G][CW];
 #pragma unroll
-                for (int g = 0; g < G; ++g)
-                    tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((acc * G + g) * npad + c0), v[g]);
+                for (int g = 0; g < G; ++g) {
+                    const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((acc * G + g) * npad + c0);
+                    if constexpr (CW == 16) tmem_ld16(ta, v[g]);
+                    else tmem_ld8(ta, v[g]);
+                }
                 tmem_wait();
                 if (!live) continue;
-                // outputs c0 .. c0 + 15: blocks c0 / P ..; one block of a row
+                // outputs c0 .. c0 + CW - 1: blocks c0 / P ..; one block of a row
                 // holds the G solves' P outputs, 8 contiguous floats
 #pragma unroll
-                for (int bb = 0; bb < 16 / P; ++bb) {
+                for (int bb = 0; bb < CW / P; ++bb) {
                     const int i0 = c0 + bb * P;
                     if (i0 >= nout) break;
                     float w[8];
@@ -416,7 +435,7 @@ bool rotate_tma(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_
     if (!(p == 1 || p == 2 || p == 4) || kc % p != 0 || kc <= 0) return false;
     const int G = 8 / p;
     const int npad = (nout + 15) / 16 * 16;
-    if (npad > 64) return false;  // two accumulator sets of G solves in 512 columns
+    if (2 * G * npad > 512) return false;  // two accumulator sets of G solves in 512 columns
     // 16-byte rules of the tensor map (base, strides) and of the 16-byte output stores
     if (((uintptr_t)V & 15) || ((uintptr_t)Vout & 15) || (ld_in * 4) % 16 || (bstride * 4) % 16 ||
         ld_out % 4 || (ostride * 4) % 16 || D > INT32_MAX)
