@@ -10,9 +10,9 @@
 //   * warp 0, one lane: per K-step (8 basis vectors = 8/p blocks) one TMA box
 //     {G p columns, 128 rows, 8/p blocks} into a ring of raw stages;
 //   * warps 2..9 (thread = row and half of the CTA's solves): split each FP32
-//     value x into two TF32 pieces, x_hi = x with its 13 low mantissa bits
-//     cleared (exact) and x_lo = tf32(x - x_hi), and store both in the UMMA
-//     K-major layout (core matrices of 8 rows x 16 bytes);
+//     value x into two TF32 pieces x_hi = tf32(x), x_lo = tf32(x - x_hi) and
+//     store both in the UMMA K-major layout (core matrices of 8 rows x 16
+//     bytes);
 //   * warp 1, one lane: per K-step and solve the three products
 //     x_hi y_hi + x_hi y_lo + x_lo y_hi as tcgen05.mma kind::tf32
 //     M=128 x N=npad x K=8 into the solve's FP32 accumulator in tensor memory
@@ -80,10 +80,13 @@ __device__ __forceinline__ float tf32_rna(float x) {
     return __uint_as_float(r);
 }
 
-// x = hi + lo with hi a TF32 value (x truncated to 10 mantissa bits, exact)
-// and lo the rest rounded to TF32: |x - hi - lo| <= 2^-21 |x|
+// x = hi + lo with hi = x rounded to TF32 and lo the (exact) rest rounded to
+// TF32: |x - hi - lo| <= 2^-22 |x|, and the dropped product lo_a lo_b has no
+// preferred sign (a truncated hi would leave a one-signed lo, whose dropped
+// products add up over the K terms: measured 3.6e-5 instead of 5e-9 on the
+// eigenvalues of the m=10 multi-sector grid)
 __device__ __forceinline__ void split2(float x, float& hi, float& lo) {
-    hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+    hi = tf32_rna(x);
     lo = tf32_rna(x - hi);
 }
 
