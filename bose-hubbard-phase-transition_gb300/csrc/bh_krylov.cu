@@ -1485,17 +1485,19 @@ static bool tc_rotation_on() {
     return v == 1;
 }
 
-// BH_TMA_ROTATE=1: the restart rotation of a batch whose solves all continue
-// streamed by TMA into warp-specialised TF32 tensor-core products
-// (bh_rotate_tma.cu) instead of the SIMT kernel
-static bool tma_rotation_on() {
+// BH_TMA_ROTATE=1 or 2: the restart rotation of a batch whose solves all
+// continue streamed by TMA into warp-specialised TF32 tensor-core products
+// (bh_rotate_tma.cu), with the split basis operand staged in shared memory (1)
+// or in tensor memory (2), instead of the SIMT kernel
+static int tma_rotation_mode() {
     static int v = -1;
     if (v < 0) {
         const char* e = std::getenv("BH_TMA_ROTATE");
-        v = (e && *e == '1') ? 1 : 0;
+        v = (e && (*e == '1' || *e == '2')) ? *e - '0' : 0;
     }
-    return v == 1;
+    return v;
 }
+static bool tma_rotation_on() { return tma_rotation_mode() != 0; }
 
 static bool debug_ortho() {
     static int v = -1;
@@ -1763,7 +1765,7 @@ struct Launcher {
             if (contiguous && !single && tma_rotation_on()) {
                 profile_begin(st);
                 if (rotate_tma(op.D, Sproc, ld_in, p, kc, nout, bstride, V, Yg, Vout, ostride, ld_out, tc_status,
-                               st)) {
+                               st, tma_rotation_mode() == 2)) {
                     done("k_rotate_tma", (double)op.D * Sproc * p * ((double)kc / p + (double)nout / p) * sizeof(T));
                     return;
                 }

@@ -275,7 +275,8 @@ bool rotate_tc(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t
 // and output solve indices the identity, not the single-array layout).
 // Returns false, launching nothing, when the shapes or alignments do not fit.
 bool rotate_tma(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t bstride, const float* V,
-                const float* Yg, float* Vout, int64_t ostride, int ld_out, int* d_status, cudaStream_t st);
+                const float* Yg, float* Vout, int64_t ostride, int ld_out, int* d_status, cudaStream_t st,
+                bool a_in_tmem);
 
 SolveResult block_lanczos(const OpView<double>& op64, const OpView<float>& op32,
                           const SolveRequest& rq, cudaStream_t st);

@@ -42,7 +42,7 @@ constexpr int RT_KS = 8;                  // TF32 values per MMA K-step
 constexpr int RT_THREADS = 448;           // 14 warps
 constexpr unsigned RT_SPIN = 1u << 24;    // polls of an mbarrier before giving up
 constexpr int RT_HEADER = 1024;           // bytes before the tiles (barriers, flags)
-constexpr int RT_MAX_RAW = 4, RT_MAX_A = 2;
+constexpr int RT_MAX_RAW = 6, RT_MAX_A = 2;
 
 // Shared-memory header: barrier indices
 enum : int {
@@ -130,6 +130,24 @@ __device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_
         : "memory");
 }
 
+// the same product with A read from tensor memory (lane = row, 8 columns of K)
+__device__ __forceinline__ void mma_tf32_ta(uint32_t dtmem, uint32_t atmem, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}" ::"r"(dtmem),
+        "r"(atmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8]) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr),
+                 "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+                 "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+                 "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+                 : "memory");
+}
+
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
                  : "memory");
@@ -158,7 +176,7 @@ __device__ __forceinline__ void tmem_wait() { asm volatile("tcgen05.wait::ld.syn
 // Shared memory (dynamic): header, B[g][piece][ks] coefficient tiles (npad
 // rows x 32 bytes), raw[NR] TMA stages ({8/p blocks}[128 rows][8 floats]),
 // A[NA][g][piece] operand tiles (128 rows x 32 bytes).
-template <int P>
+template <int P, bool ATM>
 __global__ void __launch_bounds__(RT_THREADS, 1)
 k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int kc, int nout,
              const float* __restrict__ Yg, float* __restrict__ Vout, int64_t ostride, int ld_out, int npad,
@@ -176,7 +194,7 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
     const int btile = npad * 32;
     unsigned char* sB = s_rt + RT_HEADER;
     unsigned char* sRaw = sB + (size_t)G * 2 * nks * btile;
-    unsigned char* sA = sRaw + (size_t)NR * RAW;
+    unsigned char* sA = sRaw + (size_t)NR * RAW;  // (ATM: the A stages are in tensor memory)
     auto bar = [&](int i) { return smem_u32(&bars[i]); };
 
     if (tid == 0) {
@@ -261,14 +279,21 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
                 const int slot = (int)(s % NA);
                 if (!wait_full(bar(B_A_FULL + slot), s / NA, err)) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const unsigned char* aS = sA + (size_t)slot * G * 2 * ATILE;
                 for (int g = 0; g < nsg; ++g) {
-                    const uint32_t a0 = smem_u32(aS + (size_t)g * 2 * ATILE);
                     const uint32_t b0 = smem_u32(sB + ((size_t)(g * 2) * nks + ks) * btile);
                     const uint32_t d = tmem + (uint32_t)((acc * G + g) * npad);
-                    mma_tf32(d, tile_desc(a0), tile_desc(b0), idesc, ks > 0 ? 1u : 0u);          // hi hi
-                    mma_tf32(d, tile_desc(a0), tile_desc(b0 + (uint32_t)(nks * btile)), idesc, 1u);  // hi lo
-                    mma_tf32(d, tile_desc(a0 + ATILE), tile_desc(b0), idesc, 1u);              // lo hi
+                    if constexpr (ATM) {
+                        // A pieces: 8 columns each after the accumulators
+                        const uint32_t a0 = tmem + (uint32_t)(2 * G * npad + ((slot * G + g) * 2) * 8);
+                        mma_tf32_ta(d, a0, tile_desc(b0), idesc, ks > 0 ? 1u : 0u);                      // hi hi
+                        mma_tf32_ta(d, a0, tile_desc(b0 + (uint32_t)(nks * btile)), idesc, 1u);          // hi lo
+                        mma_tf32_ta(d, a0 + 8u, tile_desc(b0), idesc, 1u);                              // lo hi
+                    } else {
+                        const uint32_t a0 = smem_u32(sA + (size_t)(slot * G + g) * 2 * ATILE);
+                        mma_tf32(d, tile_desc(a0), tile_desc(b0), idesc, ks > 0 ? 1u : 0u);              // hi hi
+                        mma_tf32(d, tile_desc(a0), tile_desc(b0 + (uint32_t)(nks * btile)), idesc, 1u);  // hi lo
+                        mma_tf32(d, tile_desc(a0 + ATILE), tile_desc(b0), idesc, 1u);                  // lo hi
+                    }
                 }
                 mma_commit(bar(B_A_EMPTY + slot));
                 if (ks == nks - 1) mma_commit(bar(B_ACC_FULL + acc));
@@ -279,9 +304,10 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
         // ---- converters: thread = row of the tile, warps 2..5 and 6..9 take
         // the first and second half of the CTA's solves ----
         constexpr int GH = G / 2;  // solves per converter thread
-        const int cw = warp - 2;
-        const int row = (cw & 3) * 32 + lane;
-        const int half = cw >> 2;
+        // row in the warp's tensor-memory lane quarter (warp w reaches lanes
+        // 32 (w % 4) .. + 31)
+        const int row = (warp & 3) * 32 + lane;
+        const int half = (warp - 2) >> 2;
         for (int64_t s = 0; s < nstep; ++s) {
             const int rs = (int)(s % NR);
             if (!wait_full(bar(B_RAW_FULL + rs), s / NR, err)) break;
@@ -297,6 +323,7 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
             if (lane == 0) bar_arrive(bar(B_RAW_EMPTY + rs));
             const int as = (int)(s % NA);
             if (!wait_empty(bar(B_A_EMPTY + as), s / NA, err)) break;
+            if constexpr (ATM) asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             unsigned char* aS = sA + (size_t)as * G * 2 * ATILE;
             const uint32_t o = tile_off(row, 0);
 #pragma unroll
@@ -306,13 +333,25 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
 #pragma unroll
                 for (int k = 0; k < 8; ++k)  // K index k = block (k / P), value k % P
                     split2(x[k / P][gg * P + k % P], hi[k], lo[k]);
-                unsigned char* ah = aS + (size_t)g * 2 * ATILE + o;
-                *reinterpret_cast<float4*>(ah) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-                *reinterpret_cast<float4*>(ah + 128) = make_float4(hi[4], hi[5], hi[6], hi[7]);
-                *reinterpret_cast<float4*>(ah + ATILE) = make_float4(lo[0], lo[1], lo[2], lo[3]);
-                *reinterpret_cast<float4*>(ah + ATILE + 128) = make_float4(lo[4], lo[5], lo[6], lo[7]);
+                if constexpr (ATM) {
+                    const uint32_t ta = tmem + ((uint32_t)((warp & 3) * 32) << 16) +
+                                        (uint32_t)(2 * G * npad + ((as * G + g) * 2) * 8);
+                    tmem_st8(ta, hi);
+                    tmem_st8(ta + 8u, lo);
+                } else {
+                    unsigned char* ah = aS + (size_t)g * 2 * ATILE + o;
+                    *reinterpret_cast<float4*>(ah) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+                    *reinterpret_cast<float4*>(ah + 128) = make_float4(hi[4], hi[5], hi[6], hi[7]);
+                    *reinterpret_cast<float4*>(ah + ATILE) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+                    *reinterpret_cast<float4*>(ah + ATILE + 128) = make_float4(lo[4], lo[5], lo[6], lo[7]);
+                }
             }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            if constexpr (ATM) {
+                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            } else {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            }
             __syncwarp();
             if (lane == 0) bar_arrive(bar(B_A_FULL + as));
         }
@@ -433,7 +472,8 @@ EncodeTiled encode_fn() {
 }  // namespace
 
 bool rotate_tma(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t bstride, const float* V,
-                const float* Yg, float* Vout, int64_t ostride, int ld_out, int* d_status, cudaStream_t st) {
+                const float* Yg, float* Vout, int64_t ostride, int ld_out, int* d_status, cudaStream_t st,
+                bool a_in_tmem) {
     if (Sproc <= 0 || D <= 0) return true;
     if (!(p == 1 || p == 2 || p == 4) || kc % p != 0 || kc <= 0) return false;
     const int G = 8 / p;
@@ -453,7 +493,11 @@ bool rotate_tma(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_
     BH_CUDA(cudaGetDevice(&dev));
     BH_CUDA(cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     int NR = RT_MAX_RAW, NA = RT_MAX_A;
-    auto smem_of = [&]() { return (size_t)RT_HEADER + bbytes + NR * raw + (size_t)NA * G * 2 * atile; };
+    // A in tensor memory when its stages fit beside the two accumulator sets
+    const bool atm = a_in_tmem && 2 * G * npad + NA * G * 16 <= 512;
+    auto smem_of = [&]() {
+        return (size_t)RT_HEADER + bbytes + NR * raw + (atm ? 0 : (size_t)NA * G * 2 * atile);
+    };
     while (smem_of() > (size_t)smax && NR > 2) --NR;
     if (smem_of() > (size_t)smax) return false;
     // the CTA takes all 512 tensor-memory columns: enough shared memory that a
@@ -482,9 +526,15 @@ bool rotate_tma(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_
         kern<<<dim3((unsigned)ngroups, (unsigned)chunks), RT_THREADS, smem, st>>>(
             tm, D, Sproc, kc, nout, Yg, Vout, ostride, ld_out, npad, nks, NR, NA, 512, tiles_per * RT_M, d_status);
     };
-    if (p == 1) launch(k_rotate_tma<1>);
-    else if (p == 2) launch(k_rotate_tma<2>);
-    else launch(k_rotate_tma<4>);
+    if (atm) {
+        if (p == 1) launch(k_rotate_tma<1, true>);
+        else if (p == 2) launch(k_rotate_tma<2, true>);
+        else launch(k_rotate_tma<4, true>);
+    } else {
+        if (p == 1) launch(k_rotate_tma<1, false>);
+        else if (p == 2) launch(k_rotate_tma<2, false>);
+        else launch(k_rotate_tma<4, false>);
+    }
     BH_CUDA(cudaGetLastError());
     return true;
 }
