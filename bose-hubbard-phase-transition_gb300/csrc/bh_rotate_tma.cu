@@ -314,11 +314,18 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
             // this row's GH P values of each of the KB blocks: 16 bytes per block
             float x[KB][4];
             const unsigned char* raw = sRaw + (size_t)rs * RAW + (size_t)row * 32 + half * 16;
+            float dep = 0.f;
 #pragma unroll
             for (int b = 0; b < KB; ++b) {
                 const float4 u = *reinterpret_cast<const float4*>(raw + (size_t)b * RT_M * 32);
                 x[b][0] = u.x; x[b][1] = u.y; x[b][2] = u.z; x[b][3] = u.w;
+                dep += (u.x + u.y) + (u.z + u.w);
             }
+            // The slot is released by one lane for the warp, and a release orders
+            // only that lane's own loads: every lane first waits for its loaded
+            // values (dep needs all of them) so that no TMA overwrites the slot
+            // while a lane's shared-memory load is still in flight.
+            asm volatile("" ::"f"(dep));
             __syncwarp();
             if (lane == 0) bar_arrive(bar(B_RAW_EMPTY + rs));
             const int as = (int)(s % NA);
