@@ -299,6 +299,12 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
                 if (ks == nks - 1) mma_commit(bar(B_ACC_FULL + acc));
                 *reinterpret_cast<volatile int*>(s_rt + OFF_NMMA) = (int)(s + 1);
             }
+            // The read-back waits for the accumulator commits only: the last
+            // operand-slot commits must also have arrived before the CTA exits,
+            // or their arrivals could land in the barriers of the next CTA on
+            // this SM.
+            for (int64_t s = nstep > NA ? nstep - NA : 0; s < nstep && !*err; ++s)
+                (void)wait_full(bar(B_A_EMPTY + (int)(s % NA)), s / NA, err);
         }
     } else if (warp < 10) {
         // ---- converters: thread = row of the tile, warps 2..5 and 6..9 take
