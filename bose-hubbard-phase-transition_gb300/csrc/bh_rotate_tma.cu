@@ -295,8 +295,17 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
                         mma_tf32(d, tile_desc(a0 + ATILE), tile_desc(b0), idesc, 1u);                  // lo hi
                     }
                 }
-                mma_commit(bar(B_A_EMPTY + slot));
-                if (ks == nks - 1) mma_commit(bar(B_ACC_FULL + acc));
+                if (ks != nks - 1) {
+                    mma_commit(bar(B_A_EMPTY + slot));
+                } else {
+                    // A tile's last step commits to the accumulator barrier only:
+                    // two commits with no product between them left the read-back
+                    // reading a tile before its last products had landed.  Its
+                    // operand slot is released once those products are complete.
+                    mma_commit(bar(B_ACC_FULL + acc));
+                    if (!wait_full(bar(B_ACC_FULL + acc), t >> 1, err)) break;
+                    bar_arrive(bar(B_A_EMPTY + slot));
+                }
                 *reinterpret_cast<volatile int*>(s_rt + OFF_NMMA) = (int)(s + 1);
             }
             // The read-back waits for the accumulator commits only: the last
