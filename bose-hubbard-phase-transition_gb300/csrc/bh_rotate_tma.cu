@@ -43,6 +43,7 @@ constexpr int RT_THREADS = 448;           // 14 warps
 constexpr unsigned RT_SPIN = 1u << 24;    // polls of an mbarrier before giving up
 constexpr int RT_HEADER = 1024;           // bytes before the tiles (barriers, flags)
 constexpr int RT_MAX_RAW = 6, RT_MAX_A = 2;
+constexpr int RT_CONV = 256;              // converter threads (warps 2..9)
 
 // Shared-memory header: barrier indices
 enum : int {
@@ -200,15 +201,15 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
     if (tid == 0) {
         for (int i = 0; i < NR; ++i) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar(B_RAW_FULL + i)));
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 8;" ::"r"(bar(B_RAW_EMPTY + i)));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar(B_RAW_EMPTY + i)), "r"(RT_CONV));
         }
         for (int i = 0; i < NA; ++i) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 8;" ::"r"(bar(B_A_FULL + i)));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar(B_A_FULL + i)), "r"(RT_CONV));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar(B_A_EMPTY + i)));
         }
         for (int i = 0; i < 2; ++i) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar(B_ACC_FULL + i)));
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;" ::"r"(bar(B_ACC_EMPTY + i)));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar(B_ACC_EMPTY + i)), "r"(RT_M));
         }
         *err = 0;
         *reinterpret_cast<volatile int*>(s_rt + OFF_NRAW) = 0;
@@ -329,20 +330,14 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
             // this row's GH P values of each of the KB blocks: 16 bytes per block
             float x[KB][4];
             const unsigned char* raw = sRaw + (size_t)rs * RAW + (size_t)row * 32 + half * 16;
-            float dep = 0.f;
 #pragma unroll
             for (int b = 0; b < KB; ++b) {
                 const float4 u = *reinterpret_cast<const float4*>(raw + (size_t)b * RT_M * 32);
                 x[b][0] = u.x; x[b][1] = u.y; x[b][2] = u.z; x[b][3] = u.w;
-                dep += (u.x + u.y) + (u.z + u.w);
             }
-            // The slot is released by one lane for the warp, and a release orders
-            // only that lane's own loads: every lane first waits for its loaded
-            // values (dep needs all of them) so that no TMA overwrites the slot
-            // while a lane's shared-memory load is still in flight.
-            asm volatile("" ::"f"(dep));
-            __syncwarp();
-            if (lane == 0) bar_arrive(bar(B_RAW_EMPTY + rs));
+            // every thread releases the slot itself: an arrive orders the
+            // arriving thread's own loads only
+            bar_arrive(bar(B_RAW_EMPTY + rs));
             const int as = (int)(s % NA);
             if (!wait_empty(bar(B_A_EMPTY + as), s / NA, err)) break;
             if constexpr (ATM) asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -368,14 +363,16 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
                     *reinterpret_cast<float4*>(ah + ATILE + 128) = make_float4(lo[4], lo[5], lo[6], lo[7]);
                 }
             }
+            // every thread makes its own writes visible to the products and
+            // arrives itself (one lane arriving for the warp after __syncwarp
+            // left other lanes' pieces unseen by the products now and then)
             if constexpr (ATM) {
                 asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             } else {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             }
-            __syncwarp();
-            if (lane == 0) bar_arrive(bar(B_A_FULL + as));
+            bar_arrive(bar(B_A_FULL + as));
         }
     } else {
         // ---- read-back: warp 10 + q reads tensor-memory lanes 32 ((10 + q) % 4) .. + 31 ----
@@ -423,8 +420,7 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            __syncwarp();
-            if (lane == 0) bar_arrive(bar(B_ACC_EMPTY + acc));
+            bar_arrive(bar(B_ACC_EMPTY + acc));
         }
     }
 
