@@ -330,13 +330,19 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
             // this row's GH P values of each of the KB blocks: 16 bytes per block
             float x[KB][4];
             const unsigned char* raw = sRaw + (size_t)rs * RAW + (size_t)row * 32 + half * 16;
+            float dep = 0.f;
 #pragma unroll
             for (int b = 0; b < KB; ++b) {
                 const float4 u = *reinterpret_cast<const float4*>(raw + (size_t)b * RT_M * 32);
                 x[b][0] = u.x; x[b][1] = u.y; x[b][2] = u.z; x[b][3] = u.w;
+                dep += (u.x + u.y) + (u.z + u.w);
             }
-            // every thread releases the slot itself: an arrive orders the
-            // arriving thread's own loads only
+            // The next TMA into this slot is an async-proxy write, which the
+            // arrive does not order after loads still in flight: every thread
+            // waits for its loaded values (dep needs all of them) and then
+            // releases the slot itself.  (Arriving right after issuing the
+            // loads let the TMA overwrite the slot under them.)
+            asm volatile("" ::"f"(dep));
             bar_arrive(bar(B_RAW_EMPTY + rs));
             const int as = (int)(s % NA);
             if (!wait_empty(bar(B_A_EMPTY + as), s / NA, err)) break;
