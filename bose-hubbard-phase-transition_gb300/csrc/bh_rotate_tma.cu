@@ -330,19 +330,24 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
             // this row's GH P values of each of the KB blocks: 16 bytes per block
             float x[KB][4];
             const unsigned char* raw = sRaw + (size_t)rs * RAW + (size_t)row * 32 + half * 16;
-            float dep = 0.f;
 #pragma unroll
             for (int b = 0; b < KB; ++b) {
                 const float4 u = *reinterpret_cast<const float4*>(raw + (size_t)b * RT_M * 32);
                 x[b][0] = u.x; x[b][1] = u.y; x[b][2] = u.z; x[b][3] = u.w;
-                dep += (u.x + u.y) + (u.z + u.w);
             }
-            // The next TMA into this slot is an async-proxy write, which the
-            // arrive does not order after loads still in flight: every thread
-            // waits for its loaded values (dep needs all of them) and then
-            // releases the slot itself.  (Arriving right after issuing the
-            // loads let the TMA overwrite the slot under them.)
-            asm volatile("" ::"f"(dep));
+            // the pieces of this thread's values, in registers before the slot is
+            // released
+            float hi[GH][8], lo[GH][8];
+#pragma unroll
+            for (int gg = 0; gg < GH; ++gg)
+#pragma unroll
+                for (int k = 0; k < 8; ++k)  // K index k = block (k / P), value k % P
+                    split2(x[k / P][gg * P + k % P], hi[gg][k], lo[gg][k]);
+            // The next TMA into this slot is an async-proxy write: every thread
+            // orders its own shared-memory loads before it with a proxy fence and
+            // releases the slot itself (an arrive alone, or one lane arriving for
+            // the warp, let the TMA overwrite values still being loaded).
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             bar_arrive(bar(B_RAW_EMPTY + rs));
             const int as = (int)(s % NA);
             if (!wait_empty(bar(B_A_EMPTY + as), s / NA, err)) break;
@@ -352,26 +357,22 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int
 #pragma unroll
             for (int gg = 0; gg < GH; ++gg) {
                 const int g = half * GH + gg;
-                float hi[8], lo[8];
-#pragma unroll
-                for (int k = 0; k < 8; ++k)  // K index k = block (k / P), value k % P
-                    split2(x[k / P][gg * P + k % P], hi[k], lo[k]);
                 if constexpr (ATM) {
                     const uint32_t ta = tmem + ((uint32_t)((warp & 3) * 32) << 16) +
                                         (uint32_t)(2 * G * npad + ((as * G + g) * 2) * 8);
-                    tmem_st8(ta, hi);
-                    tmem_st8(ta + 8u, lo);
+                    tmem_st8(ta, hi[gg]);
+                    tmem_st8(ta + 8u, lo[gg]);
                 } else {
                     unsigned char* ah = aS + (size_t)g * 2 * ATILE + o;
-                    *reinterpret_cast<float4*>(ah) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-                    *reinterpret_cast<float4*>(ah + 128) = make_float4(hi[4], hi[5], hi[6], hi[7]);
-                    *reinterpret_cast<float4*>(ah + ATILE) = make_float4(lo[0], lo[1], lo[2], lo[3]);
-                    *reinterpret_cast<float4*>(ah + ATILE + 128) = make_float4(lo[4], lo[5], lo[6], lo[7]);
+                    *reinterpret_cast<float4*>(ah) = make_float4(hi[gg][0], hi[gg][1], hi[gg][2], hi[gg][3]);
+                    *reinterpret_cast<float4*>(ah + 128) = make_float4(hi[gg][4], hi[gg][5], hi[gg][6], hi[gg][7]);
+                    *reinterpret_cast<float4*>(ah + ATILE) = make_float4(lo[gg][0], lo[gg][1], lo[gg][2], lo[gg][3]);
+                    *reinterpret_cast<float4*>(ah + ATILE + 128) =
+                        make_float4(lo[gg][4], lo[gg][5], lo[gg][6], lo[gg][7]);
                 }
             }
             // every thread makes its own writes visible to the products and
-            // arrives itself (one lane arriving for the warp after __syncwarp
-            // left other lanes' pieces unseen by the products now and then)
+            // arrives itself
             if constexpr (ATM) {
                 asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
