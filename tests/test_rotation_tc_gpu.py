@@ -1,8 +1,9 @@
 """GPU: the thick-restart rotation of the FP32 Krylov basis on the tensor
 cores -- tcgen05.mma kind::tf32 with three-piece TF32 splits (bh_rotate_tc.cu,
 BH_TC_ROTATE=1), and the TMA-streamed, warp-specialised form with two-piece
-splits (bh_rotate_tma.cu, BH_TMA_ROTATE=1, for the restarts at which every
-solve continues) -- against the SIMT rotation (the default), each in a child
+splits (bh_rotate_tma.cu, for the restarts at which every solve continues:
+the default, the split operand in tensor memory, or BH_TMA_ROTATE=1, in
+shared memory) -- against the SIMT rotation (BH_TMA_ROTATE=0), each in a child
 process because the switches are read once per process.  Every solve must give the FP64 path's
 eigenvalues within 1e-8 (pure relative), for block sizes 1, 2 and 4 (the
 tensor-core kernel's three layouts of a basis row).  Block 1 runs on the open
@@ -51,7 +52,8 @@ print(json.dumps(out))
 
 
 MODES = {"tensor cores": {"BH_TC_ROTATE": "1", "BH_TMA_ROTATE": "0"},
-         "TMA + tensor cores": {"BH_TC_ROTATE": "0", "BH_TMA_ROTATE": "1"},
+         "TMA, operand in shared memory": {"BH_TC_ROTATE": "0", "BH_TMA_ROTATE": "1"},
+         "TMA, operand in tensor memory (default)": {"BH_TC_ROTATE": "0", "BH_TMA_ROTATE": "2"},
          "SIMT": {"BH_TC_ROTATE": "0", "BH_TMA_ROTATE": "0"}}
 
 
