@@ -1487,20 +1487,27 @@ static bool tc_rotation_on() {
 
 // The restart rotation of a batch whose solves all continue runs on the
 // tensor cores, streamed by TMA (bh_rotate_tma.cu), with the split basis
-// operand in tensor memory; BH_TMA_ROTATE=1 stages that operand in shared
-// memory instead, BH_TMA_ROTATE=0 keeps the SIMT kernel.  Measured on the m=10
-// multi-sector grid (64 J x 5 sectors): 261.7 eigensolves/s against 259.3 (1)
-// and 253.3 (0), the same eigenvalues within 4.95e-9 of FP64 (4.60e-9 SIMT);
-// its rotations stream 2.4-3.0 TB/s against 1.2-1.6 TB/s.
+// operand in tensor memory, for blocks of 1 and 2; BH_TMA_ROTATE=2 (or 1,
+// the operand in shared memory) selects it for every block size,
+// BH_TMA_ROTATE=0 keeps the SIMT kernel.  Measured on the m=10 multi-sector
+// grid (64 J x 5 sectors, block 2): 261.7 eigensolves/s against 259.3 (1) and
+// 253.3 (SIMT), the same eigenvalues within 4.95e-9 of FP64 (4.60e-9 SIMT),
+// its rotations at 2.4-3.0 TB/s against 1.2-1.6 TB/s, and the same restart
+// counts.  On the 4x4 torus (block 4, four-fold levels) its rounding
+// (2^-22 per term, FP32 2^-24) took 65 restarts where SIMT took 60, so block 4
+// keeps the SIMT rotation by default.
 static int tma_rotation_mode() {
-    static int v = -1;
-    if (v < 0) {
+    static int v = -2;
+    if (v == -2) {
         const char* e = std::getenv("BH_TMA_ROTATE");
-        v = (e && (*e == '0' || *e == '1')) ? *e - '0' : 2;
+        v = (e && (*e == '0' || *e == '1' || *e == '2')) ? *e - '0' : -1;  // -1: the default
     }
     return v;
 }
-static bool tma_rotation_on() { return tma_rotation_mode() != 0; }
+static bool tma_rotation_on(int p) {
+    const int m = tma_rotation_mode();
+    return m > 0 || (m < 0 && p <= 2);
+}
 
 static bool debug_ortho() {
     static int v = -1;
@@ -1765,10 +1772,10 @@ struct Launcher {
                 int ld_out, int single, bool contiguous = false) const {
         if (Sproc <= 0) return;
         if constexpr (std::is_same<T, float>::value) {
-            if (contiguous && !single && tma_rotation_on()) {
+            if (contiguous && !single && tma_rotation_on(p)) {
                 profile_begin(st);
                 if (rotate_tma(op.D, Sproc, ld_in, p, kc, nout, bstride, V, Yg, Vout, ostride, ld_out, tc_status,
-                               st, tma_rotation_mode() == 2)) {
+                               st, tma_rotation_mode() != 1)) {
                     done("k_rotate_tma", (double)op.D * Sproc * p * ((double)kc / p + (double)nout / p) * sizeof(T));
                     return;
                 }
