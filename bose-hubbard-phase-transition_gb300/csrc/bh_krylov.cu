@@ -1766,19 +1766,16 @@ struct Launcher {
     }
     // rotation of Sproc solves (see k_rotate); Yg is Sproc x kc x nout
     // contiguous: the processed solves are 0 .. Sproc - 1 in and out (no solve
-    // retired at this restart); else omap (device, Sin entries), if given,
-    // maps each of the Sin input solves to its output position (-1: not
-    // processed), the same selection as in_idx / out_idx
+    // retired at this restart)
     void rotate(int Sproc, int ld_in, int p, int kc, int nout, int64_t bstride, const T* V,
                 const T* Yg, const int* in_idx, const int* out_idx, T* Vout, int64_t ostride,
-                int ld_out, int single, bool contiguous = false, const int* omap = nullptr,
-                int Sin = 0) const {
+                int ld_out, int single, bool contiguous = false) const {
         if (Sproc <= 0) return;
         if constexpr (std::is_same<T, float>::value) {
-            if ((contiguous || omap) && !single && tma_rotation_on(p)) {
+            if (contiguous && !single && tma_rotation_on(p)) {
                 profile_begin(st);
-                if (rotate_tma(op.D, contiguous ? Sproc : Sin, contiguous ? nullptr : omap, ld_in, p, kc, nout,
-                               bstride, V, Yg, Vout, ostride, ld_out, tc_status, st, tma_rotation_mode() != 1)) {
+                if (rotate_tma(op.D, Sproc, ld_in, p, kc, nout, bstride, V, Yg, Vout, ostride, ld_out, tc_status,
+                               st, tma_rotation_mode() != 1)) {
                     done("k_rotate_tma", (double)op.D * Sproc * p * ((double)kc / p + (double)nout / p) * sizeof(T));
                     return;
                 }
@@ -1959,7 +1956,7 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
     DevBuf<unsigned char> dead((size_t)S0 * Tdim);
     DevBuf<int> need3(1);
     BH_CUDA(cudaMemsetAsync(need3.p, 0, sizeof(int), st));
-    DevBuf<int> d_in(S0), d_out(S0), d_map(S0);
+    DevBuf<int> d_in(S0), d_out(S0);
     DevBuf<T> Yd((size_t)S0 * kmax * kmax);
     Xout.alloc((size_t)D * S0 * K);
     theta_out.assign((size_t)S0 * K, 0.0);
@@ -2321,15 +2318,11 @@ static void lanczos_phase(const OpView<T>& op, const SolveRequest& rq,
                 for (int i = 0; i < nkeep; ++i)
                     Yt[((size_t)f * kmax + c) * nkeep + i] = (T)Yh[((size_t)a * kmax + c) * kmax + i];
         }
-        // input solve -> its position in the compacted batch (-1: retired)
-        std::vector<int> omap(S, -1);
-        for (int f = 0; f < nc; ++f) omap[in[f]] = f;
         BH_CUDA(cudaMemcpyAsync(Yd.p, Yt.data(), Yt.size() * sizeof(T), cudaMemcpyHostToDevice, st));
         BH_CUDA(cudaMemcpyAsync(d_in.p, in.data(), nc * sizeof(int), cudaMemcpyHostToDevice, st));
         BH_CUDA(cudaMemcpyAsync(d_out.p, out.data(), nc * sizeof(int), cudaMemcpyHostToDevice, st));
-        BH_CUDA(cudaMemcpyAsync(d_map.p, omap.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
         L.rotate(nc, ncols, p, kmax, nkeep, bstride, Va.p, Yd.p, d_in.p, d_out.p, Vb.p, bstride2, ncols2, 0,
-                 nc == S, d_map.p, S);
+                 nc == S);
         L.gather_block(nc, p, ncols, ncols2, d_in.p, Va.p + (int64_t)nb * bstride,
                        Vb.p + (int64_t)(nkeep / p) * bstride2);
         std::swap(Va.p, Vb.p);  // equal sizes: ownership stays balanced

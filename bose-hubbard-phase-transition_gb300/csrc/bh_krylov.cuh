@@ -271,14 +271,12 @@ bool rotate_tc(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t
                const float* Yg, const int* in_idx, const int* out_idx, float* Vout, int64_t ostride,
                int ld_out, int single, int* d_status, cudaStream_t st);
 // The same rotation streamed by TMA with warp-specialised TF32 tensor-core
-// products (bh_rotate_tma.cu) at a thick restart: the Sin input solves of the
-// batch, input solve s written to output position omap[s] (-1: not rotated);
-// omap == nullptr: every solve continues in place.  Not for the single-array
-// layout.  Returns false, launching nothing, when the shapes or alignments do
-// not fit.
-bool rotate_tma(int64_t D, int Sin, const int* omap, int ld_in, int p, int kc, int nout, int64_t bstride,
-                const float* V, const float* Yg, float* Vout, int64_t ostride, int ld_out, int* d_status,
-                cudaStream_t st, bool a_in_tmem);
+// products (bh_rotate_tma.cu), for a batch whose solves all continue (input
+// and output solve indices the identity, not the single-array layout).
+// Returns false, launching nothing, when the shapes or alignments do not fit.
+bool rotate_tma(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t bstride, const float* V,
+                const float* Yg, float* Vout, int64_t ostride, int ld_out, int* d_status, cudaStream_t st,
+                bool a_in_tmem);
 
 SolveResult block_lanczos(const OpView<double>& op64, const OpView<float>& op32,
                           const SolveRequest& rq, cudaStream_t st);

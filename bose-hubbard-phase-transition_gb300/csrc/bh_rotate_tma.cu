@@ -3,11 +3,10 @@
 //
 // The rotation  out_s[:, i] = sum_{c < kc} V_s[:, c] Y_s[c][i]  (M = D rows,
 // K = kc basis vectors, N = nout kept Ritz vectors, one coefficient matrix
-// Y_s per solve) at a thick restart: the continuing solves of the batch, each
-// written to its output position (in place when every solve continues).  A
-// CTA takes G = 8 / p adjacent input solves (their columns of one basis row
-// are 32 contiguous bytes; solves that do not continue get no products) and a
-// chunk of 128-row tiles.  Warp roles:
+// Y_s per solve) of a whole batch whose solves all continue (input and output
+// solve indices are the identity).  A CTA takes G = 8 / p adjacent solves
+// (their columns of one basis row are 32 contiguous bytes) and a chunk of
+// 128-row tiles.  Warp roles:
 //   * warp 0, one lane: per K-step (8 basis vectors = 8/p blocks) one TMA box
 //     {G p columns, 128 rows, 8/p blocks} into a ring of raw stages;
 //   * warps 2..9 (thread = row and half of the CTA's solves): split each FP32
@@ -178,8 +177,8 @@ __device__ __forceinline__ void tmem_wait() { asm volatile("tcgen05.wait::ld.syn
 // A[NA][g][piece] operand tiles (128 rows x 32 bytes).
 template <int P, bool ATM>
 __global__ void __launch_bounds__(RT_THREADS, 1)
-k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sin, const int* __restrict__ omap, int kc,
-             int nout, const float* __restrict__ Yg, float* __restrict__ Vout, int64_t ostride, int ld_out, int npad,
+k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sproc, int kc, int nout,
+             const float* __restrict__ Yg, float* __restrict__ Vout, int64_t ostride, int ld_out, int npad,
              int nks, int NR, int NA, int tmem_cols, int64_t rows_per_cta, int* __restrict__ status) {
     constexpr int G = 8 / P;         // solves per CTA: G P = 8 columns = 32 bytes per row and block
     constexpr int KB = RT_KS / P;    // basis blocks per K-step
@@ -189,21 +188,8 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sin, const
     uint64_t* bars = reinterpret_cast<uint64_t*>(s_rt);
     volatile int* err = reinterpret_cast<volatile int*>(s_rt + OFF_ERR);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    // the CTA's G adjacent input solves; out[g] = the output position of
-    // solve sg0 + g (its coefficient matrix and output columns), -1 for a
-    // solve that is not rotated (retired, or past the batch); omap == nullptr:
-    // every input solve continues in place
     const int sg0 = blockIdx.x * G;
-    int out[G];
-    bool any = false;
-#pragma unroll
-    for (int g = 0; g < G; ++g) {
-        const int si = sg0 + g;
-        out[g] = si < Sin ? (omap ? omap[si] : si) : -1;
-        any |= out[g] >= 0;
-    }
-    if (!any) return;  // uniform over the CTA: nothing allocated or initialised yet
-    const bool in_place = omap == nullptr && sg0 + G <= Sin;
+    const int nsg = min(G, Sproc - sg0);
     const int btile = npad * 32;
     unsigned char* sB = s_rt + RT_HEADER;
     unsigned char* sRaw = sB + (size_t)G * 2 * nks * btile;
@@ -240,11 +226,7 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sin, const
     for (int e = tid; e < G * kcp * npad; e += blockDim.x) {
         const int g = e / (kcp * npad), rem = e - g * (kcp * npad);
         const int c = rem / npad, o = rem - c * npad;
-        int og = -1;
-#pragma unroll
-        for (int q = 0; q < G; ++q)
-            if (q == g) og = out[q];
-        const float y = (og >= 0 && c < kc && o < nout) ? Yg[((size_t)og * kc + c) * nout + o] : 0.f;
+        const float y = (g < nsg && c < kc && o < nout) ? Yg[((size_t)(sg0 + g) * kc + c) * nout + o] : 0.f;
         float y0, y1;
         split2(y, y0, y1);
         unsigned char* base = sB + ((size_t)(g * 2) * nks + c / RT_KS) * btile + tile_off(o, c & 7);
@@ -296,9 +278,7 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sin, const
                 const int slot = (int)(s % NA);
                 if (!wait_full(bar(B_A_FULL + slot), s / NA, err)) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-                for (int g = 0; g < G; ++g) {
-                    if (out[g] < 0) continue;
+                for (int g = 0; g < nsg; ++g) {
                     const uint32_t b0 = smem_u32(sB + ((size_t)(g * 2) * nks + ks) * btile);
                     const uint32_t d = tmem + (uint32_t)((acc * G + g) * npad);
                     if constexpr (ATM) {
@@ -433,17 +413,14 @@ k_rotate_tma(const __grid_constant__ CUtensorMap tmap, int64_t D, int Sin, const
                     for (int g = 0; g < G; ++g)
 #pragma unroll
                         for (int q = 0; q < P; ++q) w[g * P + q] = __uint_as_float(v[g][bb * P + q]);
-                    float* row_out = Vout + (int64_t)(i0 / P) * ostride + r * ld_out;
-                    if (in_place) {
-                        float* dst = row_out + (int64_t)sg0 * P;
+                    float* dst = Vout + (int64_t)(i0 / P) * ostride + r * ld_out + (int64_t)sg0 * P;
+                    if (nsg == G) {
                         reinterpret_cast<float4*>(dst)[0] = make_float4(w[0], w[1], w[2], w[3]);
                         reinterpret_cast<float4*>(dst)[1] = make_float4(w[4], w[5], w[6], w[7]);
                     } else {
 #pragma unroll
-                        for (int g = 0; g < G; ++g)
-                            if (out[g] >= 0)
-#pragma unroll
-                                for (int q = 0; q < P; ++q) row_out[(int64_t)out[g] * P + q] = w[g * P + q];
+                        for (int e = 0; e < 8; ++e)
+                            if (e < nsg * P) dst[e] = w[e];
                     }
                 }
             }
@@ -517,18 +494,18 @@ EncodeTiled encode_fn() {
 
 }  // namespace
 
-bool rotate_tma(int64_t D, int Sin, const int* omap, int ld_in, int p, int kc, int nout, int64_t bstride,
-                const float* V, const float* Yg, float* Vout, int64_t ostride, int ld_out, int* d_status,
-                cudaStream_t st, bool a_in_tmem) {
-    if (Sin <= 0 || D <= 0) return true;
+bool rotate_tma(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_t bstride, const float* V,
+                const float* Yg, float* Vout, int64_t ostride, int ld_out, int* d_status, cudaStream_t st,
+                bool a_in_tmem) {
+    if (Sproc <= 0 || D <= 0) return true;
     if (!(p == 1 || p == 2 || p == 4) || kc % p != 0 || kc <= 0) return false;
     const int G = 8 / p;
     const int npad = (nout + 15) / 16 * 16;
     if (2 * G * npad > 512) return false;  // two accumulator sets of G solves in 512 columns
     // 16-byte rules of the tensor map (base, strides) and of the 16-byte output stores
-    if (((uintptr_t)V & 15) || (ld_in * 4) % 16 || (bstride * 4) % 16 || D > INT32_MAX) return false;
-    // the 16-byte stores of a solve group written in place
-    if (!omap && (((uintptr_t)Vout & 15) || ld_out % 4 || (ostride * 4) % 16)) return false;
+    if (((uintptr_t)V & 15) || ((uintptr_t)Vout & 15) || (ld_in * 4) % 16 || (bstride * 4) % 16 ||
+        ld_out % 4 || (ostride * 4) % 16 || D > INT32_MAX)
+        return false;
     const EncodeTiled enc = encode_fn();
     if (!enc) return false;
     const int nks = (kc + RT_KS - 1) / RT_KS;
@@ -560,7 +537,7 @@ bool rotate_tma(int64_t D, int Sin, const int* omap, int ld_in, int p, int kc, i
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return false;
 
-    const int ngroups = (Sin + G - 1) / G;
+    const int ngroups = (Sproc + G - 1) / G;
     const int64_t tiles = (D + RT_M - 1) / RT_M;
     int64_t chunks = std::max<int64_t>(1, ((int64_t)2 * sm_count() + ngroups - 1) / ngroups);
     chunks = std::min(chunks, tiles);
@@ -570,8 +547,7 @@ bool rotate_tma(int64_t D, int Sin, const int* omap, int ld_in, int p, int kc, i
     auto launch = [&](auto kern) {
         allow_large_smem(kern, smem);
         kern<<<dim3((unsigned)ngroups, (unsigned)chunks), RT_THREADS, smem, st>>>(
-            tm, D, Sin, omap, kc, nout, Yg, Vout, ostride, ld_out, npad, nks, NR, NA, 512, tiles_per * RT_M,
-            d_status);
+            tm, D, Sproc, kc, nout, Yg, Vout, ostride, ld_out, npad, nks, NR, NA, 512, tiles_per * RT_M, d_status);
     };
     if (atm) {
         if (p == 1) launch(k_rotate_tma<1, true>);
