@@ -73,7 +73,7 @@ EXPORTS = [
     "bh_hamiltonian_create_matrix_free", "bh_hamiltonian_is_matrix_free",
     "bh_hamiltonian_destroy", "bh_hamiltonian_nnz", "bh_hamiltonian_csr", "bh_hamiltonian_multi_csr",
     "bh_hamiltonian_apply", "bh_hamiltonian_apply_noalloc", "bh_solver_opts_default", "bh_eigsh", "bh_eigsh_csr",
-    "bh_eigsh_batch", "bh_eigsh_batch_status", "bh_eigsh_batch_vectors", "bh_eigsh_batch_sectors", "bh_dense_eigh", "bh_gap_ratios", "bh_spdm", "bh_phase_map", "bh_scmf", "bh_mean_field_grid", "bh_profile_enable",
+    "bh_eigsh_batch", "bh_eigsh_batch_status", "bh_eigsh_batch_vectors", "bh_eigsh_batch_sectors", "bh_folm_diag_csr", "bh_dense_eigh", "bh_gap_ratios", "bh_spdm", "bh_phase_map", "bh_scmf", "bh_mean_field_grid", "bh_profile_enable",
     "bh_profile_reset", "bh_profile_count", "bh_profile_get",
     "bh_spmm_candidates", "bh_hamiltonian_apply_shape", "bh_spmm_autotune", "bh_spmm_tuning_count",
     "bh_spmm_tuning_get", "bh_spmm_tuning_reset",
@@ -128,6 +128,7 @@ def load() -> C.CDLL:
                                          vp, C.POINTER(bh_solve_info)]
     L.bh_eigsh_batch_sectors.argtypes = [C.c_int, vp, C.c_int, vp, vp, vp, C.POINTER(bh_solver_opts), vp, vp, vp,
                                          C.POINTER(bh_solve_info)]
+    L.bh_folm_diag_csr.argtypes = [C.c_int64, vp, vp, vp, C.c_int, vp, vp, vp, vp]
     L.bh_dense_eigh.argtypes = [C.c_int64, vp, vp, vp]
     L.bh_gap_ratios.argtypes = [C.c_int, vp, vp, f64p]
     L.bh_spdm.argtypes = [vp, C.c_int, vp, vp]
@@ -719,6 +720,33 @@ class Op:
         _check(rc)
         order = np.argsort(-np.abs(ev), kind="stable")
         return ev[order].astype(complex), vec[order].T.astype(complex)
+
+    @staticmethod
+    def FOLM_diag(O, nb_iter: int, v_0):
+        """Op::FOLM_diag (operator.cpp:39-71): nb_iter Lanczos steps of the
+        symmetric O from v_0 with full re-orthogonalisation, on the device in
+        FP64 (bh_folm_diag_csr).  v_0 (float64 array) is normalised in place, as
+        the reference does.  Returns T [nb_iter, nb_iter] (tridiagonal, zeros
+        beyond the steps taken), V [D, nb_iter] (the Krylov vectors as
+        columns, zeros beyond) and the number of steps (fewer than nb_iter
+        after a breakdown, beta < 1e-6)."""
+        import scipy.sparse as sp
+
+        A = sp.csr_matrix(O)
+        A.sort_indices()
+        D = A.shape[0]
+        if not (isinstance(v_0, np.ndarray) and v_0.dtype == np.float64 and v_0.flags.c_contiguous
+                and v_0.shape == (D,)):
+            raise TypeError("v_0 must be a contiguous float64 array of the matrix dimension")
+        rp = np.ascontiguousarray(A.indptr, np.int64)
+        ci = np.ascontiguousarray(A.indices, np.int32)
+        val = np.ascontiguousarray(A.data, np.float64)
+        T = np.zeros((nb_iter, nb_iter))
+        V = np.zeros((nb_iter, D))  # column j of the reference's V is row j here
+        steps = C.c_int()
+        _check(load().bh_folm_diag_csr(D, _ptr(rp), _ptr(ci), _ptr(val), int(nb_iter), _ptr(v_0), _ptr(T),
+                                       _ptr(V), C.byref(steps)))
+        return T, np.ascontiguousarray(V.T), steps.value
 
     @staticmethod
     def FOLM_eigen(O, nb_iter: int, **opt):

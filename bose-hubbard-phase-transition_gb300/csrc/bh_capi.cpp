@@ -610,6 +610,44 @@ int bh_eigsh_csr(int64_t dim, const int64_t* row_ptr, const int32_t* col, const 
     });
 }
 
+int bh_folm_diag_csr(int64_t dim, const int64_t* row_ptr, const int32_t* col, const double* val, int nb_iter,
+                     double* v0, double* T, double* V, int* steps) {
+    return guard([&] {
+        BH_REQUIRE(dim >= 1 && dim <= 2147483647LL, "dimension out of range");
+        BH_REQUIRE(row_ptr && col && val && v0 && T && V, "null argument");
+        BH_REQUIRE(nb_iter >= 1 && nb_iter <= dim, "nb_iter must be in [1, dimension]");
+        BH_REQUIRE(row_ptr[0] == 0, "row_ptr[0] must be 0");
+        const int64_t nnz = row_ptr[dim];
+        for (int64_t r = 0; r < dim; ++r) BH_REQUIRE(row_ptr[r + 1] >= row_ptr[r], "row_ptr must be non-decreasing");
+        for (int64_t e = 0; e < nnz; ++e) BH_REQUIRE(col[e] >= 0 && col[e] < dim, "column index out of range");
+        require_finite(val, nnz, "matrix values");
+        require_finite(v0, dim, "start vector");
+        double n2 = 0.0;
+        for (int64_t r = 0; r < dim; ++r) n2 += v0[r] * v0[r];
+        BH_REQUIRE(n2 > 0.0, "start vector is zero");
+        // the reference normalises the caller's v_0 in place (operator.cpp:43)
+        const double inv = 1.0 / std::sqrt(n2);
+        for (int64_t r = 0; r < dim; ++r) v0[r] *= inv;
+        Stream st;
+        DevBuf<int64_t> rp(dim + 1);
+        DevBuf<int32_t> ci(nnz);
+        DevBuf<double> v64(nnz);
+        BH_CUDA(cudaMemcpyAsync(rp.p, row_ptr, (dim + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+        if (nnz) {
+            BH_CUDA(cudaMemcpyAsync(ci.p, col, nnz * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+            BH_CUDA(cudaMemcpyAsync(v64.p, val, nnz * sizeof(double), cudaMemcpyHostToDevice, st));
+        }
+        OpView<double> a64;
+        a64.rp = rp.p;
+        a64.ci = ci.p;
+        a64.tv = v64.p;
+        a64.D = dim;
+        a64.rp_nnz = nnz;
+        const int k = folm_diag(a64, nb_iter, v0, T, V, st);
+        if (steps) *steps = k;
+    });
+}
+
 int bh_dense_eigh(int64_t n, const double* a, double* w, double* z) {
     return guard([&] {
         BH_REQUIRE(a && w, "null argument");

@@ -2650,3 +2650,63 @@ SolveResult block_lanczos(const OpView<double>& op64, const OpView<float>& op32,
 }
 
 }  // namespace bh
+
+namespace bh {
+
+// Op::FOLM_diag (operator.cpp:39-71) as its comments describe it: nb_iter
+// Lanczos steps from v0 in FP64 with full re-orthogonalisation.  Step i forms
+// w = O v_i, removes its components along every vector so far (v_i included)
+// with two classical Gram-Schmidt passes, and sets T_ii = alpha_i (the v_i
+// coefficients of both passes) and T_{i,i+1} = T_{i+1,i} = beta_i = |w|,
+// v_{i+1} = w / beta_i; it stops after nb_iter vectors or once beta_i < 1e-6
+// (the reference's threshold).  T is k x k (zeros beyond the steps taken), V
+// column-major D x k.  Returns the number of vectors.  (The reference's loop
+// leaves v_i out of the orthogonalisation and stores beta_i one row late;
+// callers of the API get the tridiagonal matrix the method defines.)
+int folm_diag(const OpView<double>& op, int k, const double* v0, double* T, double* V, cudaStream_t st) {
+    const int64_t D = op.D;
+    int64_t launches = 0;
+    Launcher<double> L{op, st, &launches};
+    const Geo g = make_geo(D, 1), gu = make_ugeo(D, 1);
+    const int kcap = k + 1;
+    DevBuf<double> Vd((size_t)k * D), W((size_t)D), prm(3), part((size_t)g.nchunks * kcap), C((size_t)kcap),
+        Cf((size_t)kcap), rinv(1);
+    const double hp[3] = {1.0, 0.0, 0.0};  // J, U, shift: the product is O itself
+    BH_CUDA(cudaMemcpyAsync(prm.p, hp, sizeof hp, cudaMemcpyHostToDevice, st));
+    BH_CUDA(cudaMemcpyAsync(Vd.p, v0, (size_t)D * sizeof(double), cudaMemcpyHostToDevice, st));
+    std::fill(T, T + (size_t)k * k, 0.0);
+    auto read = [&](const double* dsrc) {
+        double h = 0.0;
+        BH_CUDA(cudaMemcpyAsync(&h, dsrc, sizeof(double), cudaMemcpyDeviceToHost, st));
+        BH_CUDA(cudaStreamSynchronize(st));
+        return h;
+    };
+    int steps = 0;
+    for (int i = 0; i < k; ++i) {
+        L.spmm(1, 1, prm.p, Vd.p + (int64_t)i * D, W.p);
+        double alpha = 0.0;
+        for (int pass = 0; pass < 2; ++pass) {
+            L.dot(g, 1, 1, i + 1, D, Vd.p, W.p, kcap, part.p);
+            L.dot_finalize(g, i + 1, 1, 1, kcap, part.p, C.p, Cf.p, nullptr, 0, 0);
+            L.update(gu, 1, i + 1, D, Vd.p, Cf.p, W.p, 0, nullptr);
+            alpha += read(C.p + i);
+        }
+        L.dot(g, 1, 1, 1, D, W.p, W.p, kcap, part.p);
+        L.dot_finalize(g, 1, 1, 1, kcap, part.p, C.p, nullptr, nullptr, 0, 0);
+        const double beta = std::sqrt(std::max(read(C.p), 0.0));
+        T[(size_t)i * k + i] = alpha;
+        steps = i + 1;
+        if (i + 1 == k || !(beta >= 1e-6)) break;
+        T[(size_t)i * k + i + 1] = beta;
+        T[(size_t)(i + 1) * k + i] = beta;
+        const double r = 1.0 / beta;
+        BH_CUDA(cudaMemcpyAsync(rinv.p, &r, sizeof r, cudaMemcpyHostToDevice, st));
+        L.normalize(1, 1, rinv.p, W.p, Vd.p + (int64_t)(i + 1) * D);
+    }
+    BH_CUDA(cudaMemcpyAsync(V, Vd.p, (size_t)steps * D * sizeof(double), cudaMemcpyDeviceToHost, st));
+    BH_CUDA(cudaStreamSynchronize(st));
+    std::fill(V + (size_t)steps * D, V + (size_t)k * D, 0.0);
+    return steps;
+}
+
+}  // namespace bh

@@ -278,6 +278,12 @@ bool rotate_tma(int64_t D, int Sproc, int ld_in, int p, int kc, int nout, int64_
                 const float* Yg, float* Vout, int64_t ostride, int ld_out, int* d_status, cudaStream_t st,
                 bool a_in_tmem);
 
+// Op::FOLM_diag: k Lanczos steps of the FP64 operator from v0 (unit norm, host)
+// with full re-orthogonalisation; T (k x k, host) and V (D x k column-major,
+// host) receive the tridiagonal matrix and the Krylov vectors.  Returns the
+// number of vectors (fewer than k after a breakdown, beta < 1e-6).
+int folm_diag(const OpView<double>& op, int k, const double* v0, double* T, double* V, cudaStream_t st);
+
 SolveResult block_lanczos(const OpView<double>& op64, const OpView<float>& op32,
                           const SolveRequest& rq, cudaStream_t st);
 

@@ -152,4 +152,26 @@ inline void irlm_eigen(const Csr& O, int nev, std::vector<double>& vals, std::ve
     }
 }
 
+// Op::FOLM_diag (operator.cpp:39-71): nb_iter Lanczos steps of O from v0
+// (normalised in place) with full re-orthogonalisation; T (nb_iter x nb_iter)
+// and V (O.dim x nb_iter), both column-major, receive the tridiagonal matrix
+// and the Krylov vectors.  Returns the number of vectors.
+inline int folm_diag(const Csr& O, int nb_iter, std::vector<double>& v0, std::vector<double>& T,
+                     std::vector<double>& V) {
+    if (nb_iter < 1 || nb_iter > O.dim) throw std::invalid_argument("nb_iter must satisfy 1 <= nb_iter <= n");
+    if ((int64_t)v0.size() != O.dim) throw std::invalid_argument("v_0 must have the size of the matrix");
+    T.assign((size_t)nb_iter * nb_iter, 0.0);
+    V.assign((size_t)nb_iter * O.dim, 0.0);
+    std::vector<int32_t> ci(O.ci);
+    std::vector<double> val(O.val);
+    if (ci.empty()) {
+        ci.push_back(0);
+        val.push_back(0.0);
+    }
+    int steps = 0;
+    check(bh_folm_diag_csr(O.dim, O.rp.data(), ci.data(), val.data(), nb_iter, v0.data(), T.data(), V.data(),
+                           &steps));
+    return steps;
+}
+
 }  // namespace bhgb

@@ -242,6 +242,20 @@ int bh_eigsh_batch_sectors(int nh, const bh_hamiltonian* const* hs, int nsolve, 
                            const double* U, const double* mu, const bh_solver_opts* o,
                            double* evals, double* resid, int* nconv, bh_solve_info* info);
 
+/* Replaces Op::FOLM_diag (operator.cpp:39-71): nb_iter Lanczos steps of the
+ * symmetric CSR matrix (host arrays, as bh_eigsh_csr) from the start vector
+ * v0[dim] (normalised in place, as the reference does), FP64 with full
+ * re-orthogonalisation of every new vector against all earlier ones.
+ * T[nb_iter * nb_iter] receives the tridiagonal matrix (T_ii = alpha_i,
+ * T_{i,i+1} = T_{i+1,i} = beta_i, zeros beyond the steps taken) and
+ * V[nb_iter * dim] the Krylov vectors as columns (V[j * dim + r], column-major
+ * like Eigen::MatrixXd); *steps (optional) the number of vectors: fewer than
+ * nb_iter once beta_i < 1e-6 (the reference's breakdown test).  The
+ * reference's own loop leaves v_i out of the orthogonalisation and stores
+ * beta_i one row late; this gives the matrix the method defines. */
+int bh_folm_diag_csr(int64_t dim, const int64_t* row_ptr, const int32_t* col, const double* val, int nb_iter,
+                     double* v0, double* T, double* V, int* steps);
+
 /* Replaces Op::exact_eigen (operator.cpp:92-101): all eigenvalues (ascending)
  * and, if z != NULL, eigenvectors (columns of z, column-major n x n) of the
  * dense symmetric matrix a (column-major, host).  n <= 32768. */

@@ -232,6 +232,15 @@ Eigen::VectorXcd Op::IRLM_eigen(Eigen::SparseMatrix<double> O, int nb_eigen, Eig
 
 // The intended full-orthogonalisation Lanczos: the lowest
 // min(nb_iter, n - 2, 32) eigenpairs, ascending, FP64.
+void Op::FOLM_diag(Eigen::SparseMatrix<double> O, int nb_iter, Eigen::VectorXd& v_0, Eigen::MatrixXd& T,
+                   Eigen::MatrixXd& V) {
+    std::vector<double> v0(v_0.data(), v_0.data() + v_0.size()), t, vv;
+    bhgb::folm_diag(bhgb::csr_of(O), nb_iter, v0, t, vv);
+    for (Eigen::Index r = 0; r < v_0.size(); ++r) v_0[r] = v0[(size_t)r];  // normalised, as the reference's
+    T = Eigen::Map<Eigen::MatrixXd>(t.data(), nb_iter, nb_iter);
+    V = Eigen::Map<Eigen::MatrixXd>(vv.data(), O.rows(), nb_iter);
+}
+
 Eigen::VectorXd Op::FOLM_eigen(Eigen::SparseMatrix<double> O, int nb_iter, Eigen::MatrixXd& eigenvectors) {
     const int nev = std::max(1, std::min<int>({nb_iter, (int)O.rows() - 2, 32}));
     std::vector<double> ev, vec;

@@ -46,5 +46,5 @@ def test_reference_program_links_against_the_dropin(tmp_path, pkg):
     for sym in ["BH::fixed_set_basis", "BH::fixed_bosons_hamiltonian", "BH::max_bosons_hamiltonian",
                 "BH::max_set_basis", "BH::calculate_tag", "BH::search_tag", "BH::h_MF",
                 "Neighbours::chain_neighbours", "Neighbours::square_neighbours",
-                "Neighbours::getNeighbours", "Op::IRLM_eigen", "Op::FOLM_eigen", "Op::exact_eigen"]:
+                "Neighbours::getNeighbours", "Op::IRLM_eigen", "Op::FOLM_diag", "Op::FOLM_eigen", "Op::exact_eigen"]:
         assert sym in nm, sym
