@@ -10,8 +10,13 @@
 //   same <k> <0|1>      1 if the concurrent values equal a sequential re-run bit for bit
 //   noconv <k> <what>   the exception text of a solve capped at 1 restart of a 22-vector basis
 //   badarg <what>       the exception text of nev = n - 1
+//   folm <steps> <max|V^T V - I|> <alpha_0..alpha_k-1> <beta_0..beta_k-2>
+//                       Op::FOLM_diag through the C++ layer: 30 Lanczos steps of
+//                       point 0 from v0[r] = sin(0.37 (r + 1))
 #include <omp.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <stdexcept>
@@ -82,6 +87,24 @@ int main(int argc, char** argv) {
         std::printf("badarg no exception\n");
     } catch (const std::invalid_argument& e) {
         std::printf("badarg %s\n", e.what());
+    }
+    {
+        const bhgb::Csr& O = ops[0];
+        const int k = 30;
+        std::vector<double> v0((size_t)O.dim), T, V;
+        for (int64_t r = 0; r < O.dim; ++r) v0[(size_t)r] = std::sin(0.37 * (double)(r + 1));
+        const int steps = bhgb::folm_diag(O, k, v0, T, V);
+        double orth = 0.0;
+        for (int a = 0; a < steps; ++a)
+            for (int c = 0; c < steps; ++c) {
+                double d = 0.0;
+                for (int64_t r = 0; r < O.dim; ++r) d += V[(size_t)a * O.dim + r] * V[(size_t)c * O.dim + r];
+                orth = std::max(orth, std::fabs(d - (a == c ? 1.0 : 0.0)));
+            }
+        std::printf("folm %d %.3e", steps, orth);
+        for (int i = 0; i < k; ++i) std::printf(" %.17g", T[(size_t)i * k + i]);
+        for (int i = 0; i + 1 < k; ++i) std::printf(" %.17g", T[(size_t)i * k + i + 1]);
+        std::printf("\n");
     }
     return 0;
 }

@@ -57,3 +57,13 @@ def test_concurrent_irlm_eigen_like_the_reference_grid_loop(driver, golden):
     assert noconv == ["Eigenvalue computation failed."] * nthreads
     badarg = [l for l in lines if l.startswith("badarg ")]
     assert badarg == ["badarg nev must satisfy 1 <= nev <= n - 2, n is the size of matrix"]
+    # Op::FOLM_diag through the C++ layer: orthonormal Krylov vectors and a
+    # tridiagonal matrix whose lowest Ritz value has reached the ground state
+    folm = [l.split() for l in lines if l.startswith("folm ")]
+    assert len(folm) == 1
+    steps, orth = int(folm[0][1]), float(folm[0][2])
+    vals = np.array([float(x) for x in folm[0][3:]])
+    assert steps == 30 and orth < 1e-12
+    T = np.diag(vals[:30]) + np.diag(vals[30:], 1) + np.diag(vals[30:], -1)
+    e0 = np.min(got)
+    assert abs(np.linalg.eigvalsh(T)[0] - e0) < 1e-7 * abs(e0)
