@@ -58,12 +58,14 @@ def test_concurrent_irlm_eigen_like_the_reference_grid_loop(driver, golden):
     badarg = [l for l in lines if l.startswith("badarg ")]
     assert badarg == ["badarg nev must satisfy 1 <= nev <= n - 2, n is the size of matrix"]
     # Op::FOLM_diag through the C++ layer: orthonormal Krylov vectors and a
-    # tridiagonal matrix whose lowest Ritz value has reached the ground state
+    # tridiagonal matrix whose lowest Ritz value approaches the ground state
+    # from above (30 steps from this start: 2.9e-6 relative; the 40-step
+    # convergence check is in tests/test_folm_gpu.py)
     folm = [l.split() for l in lines if l.startswith("folm ")]
     assert len(folm) == 1
     steps, orth = int(folm[0][1]), float(folm[0][2])
     vals = np.array([float(x) for x in folm[0][3:]])
     assert steps == 30 and orth < 1e-12
     T = np.diag(vals[:30]) + np.diag(vals[30:], 1) + np.diag(vals[30:], -1)
-    e0 = np.min(got)
-    assert abs(np.linalg.eigvalsh(T)[0] - e0) < 1e-7 * abs(e0)
+    e0, ritz0 = np.min(got), np.linalg.eigvalsh(T)[0]
+    assert e0 - 1e-12 * abs(e0) <= ritz0 < e0 + 1e-4 * abs(e0)
