@@ -22,6 +22,9 @@ on the device.
                sample of the grid, for the batched-vs-plain ratio
   accuracy     max relative eigenvalue error of the mixed results vs FP64
   roofline     dominant kernel, algorithmic bytes / CUDA-event duration
+  whole_solver every kernel's algorithmic bytes of one step over the summed
+               kernel time and over the step time
+  spmm_gather  the sparse product against the bytes it must gather
   cpu_baseline the CPU oracle's restatement of the reference's IRLM
                (OpenMP over points) on a bounded sample of the grid
 Reference arm (--impl reference): the CPU restatement alone, timed per step
@@ -422,6 +425,17 @@ def run_ours(args):
                            "algorithmic_bytes_per_launch": round(per_launch_bytes)}
         out["kernel_time_shares"] = {k: round(v["ms"] / tot_ms, 4)
                                      for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])}
+        # the whole solver against the same roofline: every kernel's
+        # algorithmic bytes of one step over the summed kernel time, and over
+        # the timed step (the sectors overlap on the device)
+        tot_bytes = sum(v["bytes"] for v in prof.values())
+        out["whole_solver"] = {
+            "algorithmic_bytes_per_step": round(tot_bytes),
+            "kernel_ms_per_step": round(tot_ms, 1),
+            "gbs_over_kernel_time": round(tot_bytes / (tot_ms * 1e6), 1),
+            "gbs_over_step_time": round(tot_bytes / (t_val / args.steps * 1e9), 1),
+            "peak": peak, "peak_kind": peak_kind,
+            "frac_over_step_time": round(tot_bytes / (t_val / args.steps * 1e9) / peak, 4)}
         out["kernel_gbs"] = {k: round(v["bytes"] / (v["ms"] * 1e6), 1)
                              for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"]) if v["ms"] > 0}
 
