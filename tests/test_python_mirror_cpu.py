@@ -166,3 +166,15 @@ def test_folm_eigen_clamps_and_orders(pkg, monkeypatch):
     assert calls[-1] == 10 and np.array_equal(vals, w[:10])  # n - 2
     pkg.Op.FOLM_eigen(A, 0)
     assert calls[-1] == 1
+
+
+def test_folm_diag_checks_its_start_vector_before_the_device(pkg):
+    # v_0 is normalised in place by the library, so it must be the caller's own
+    # contiguous float64 array of the matrix dimension: anything else is
+    # refused on the host, before any library call
+    import scipy.sparse as sp
+
+    H = sp.diags(np.arange(1.0, 5.0)).tocsr()
+    for bad in (np.ones(4, np.float32), np.ones(5), np.ones((4, 1)), np.ones(8)[::2], [1.0, 0.0, 0.0, 0.0]):
+        with pytest.raises(TypeError):
+            pkg.Op.FOLM_diag(H, 2, bad)
