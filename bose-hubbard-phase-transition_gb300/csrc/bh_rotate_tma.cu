@@ -11,8 +11,9 @@
 //     {G p columns, 128 rows, 8/p blocks} into a ring of raw stages;
 //   * warps 2..9 (thread = row and half of the CTA's solves): split each FP32
 //     value x into two TF32 pieces x_hi = tf32(x), x_lo = tf32(x - x_hi) and
-//     store both in the UMMA K-major layout (core matrices of 8 rows x 16
-//     bytes);
+//     store both in tensor memory (tcgen05.st, lane = row, 8 columns of K;
+//     ATM) or in shared memory in the UMMA K-major layout (core matrices of 8
+//     rows x 16 bytes);
 //   * warp 1, one lane: per K-step and solve the three products
 //     x_hi y_hi + x_hi y_lo + x_lo y_hi as tcgen05.mma kind::tf32
 //     M=128 x N=npad x K=8 into the solve's FP32 accumulator in tensor memory
@@ -21,12 +22,18 @@
 //   * warps 10..13 (thread = row): read a finished tile's accumulators with
 //     tcgen05.ld and write the G solves' outputs of one block of a row as two
 //     16-byte stores.
-// The dropped product x_lo y_lo and the truncation of the pieces leave a
-// relative error of about 2^-21 per product term, the order of FP32 rounding
-// of the accumulated sum.  Every mbarrier wait is bounded: on a timeout the
-// CTA records an error flag, every role stops, the producer and the MMA
-// thread wait (bounded) for their operations in flight, and the tensor memory
-// is freed.
+// The dropped product x_lo y_lo and the rounding of the pieces leave a
+// relative error of at most about 2^-22 per product term, below the FP32
+// rounding of the accumulated sum.
+// Ordering: every consumer thread releases a ring stage itself -- a raw stage
+// after a proxy fence that orders its loads before the next TMA write -- and
+// every converter thread publishes its own pieces (fence, then arrive); each
+// K-step commits to one barrier (a tile's last step to the accumulator
+// barrier, whose arrival then releases its operand stage); the MMA thread
+// waits for its last commits before the CTA exits.  Every mbarrier wait is
+// bounded: on a timeout the CTA records an error flag, every role stops, the
+// producer and the MMA thread wait (bounded) for their operations in flight,
+// and the tensor memory is freed.
 #include <cuda.h>
 
 #include <cstdint>
